@@ -1,0 +1,172 @@
+"""ctypes bindings of the CPU oracle (depix_oracle.c) and, when it has been
+built in this checkout, of the host build of the reference's own stage bodies
+(oracle/_ref). TEST INFRASTRUCTURE ONLY: imported by tests/, by
+__graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by the
+product library.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdepix_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+CELL = 45
+
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with IEEE semantics (no FMA contraction)."""
+    src = os.path.join(HERE, "depix_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                               "-o", LIB_PATH, src, "-lm"])
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_yuv_word.restype = ctypes.c_uint32
+        L.orc_yuv_word.argtypes = [ctypes.c_uint8] * 3
+        L.orc_graph.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, _u8p]
+        L.orc_trivial.argtypes = [_u8p, ctypes.c_int, ctypes.c_int]
+        L.orc_heuristics.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u8p]
+        L.orc_hull_table.argtypes = [_i32p, _i8p]
+        L.orc_raster.argtypes = [_f32p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u8p]
+        L.orc_label_cc.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _i32p]
+        vp = ctypes.c_void_p
+        L.orc_frame.restype = ctypes.c_int
+        L.orc_frame.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, ctypes.c_int] + [vp] * 9
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Frame:
+    """All outputs of one run of the path on one frame."""
+
+    def __init__(self, w, h):
+        n = w * h
+        self.w, self.h = w, h
+        self.graph_trivial = np.zeros(n, np.uint8)
+        self.graph = np.zeros(n, np.uint8)
+        self.ec_cells = np.zeros(n, np.int32)
+        self.diag_cells = np.zeros(n * CELL * 2, np.float32)
+        self.ec = np.zeros(n, np.int32)
+        self.diag = np.zeros(n * CELL * 2, np.float32)
+        self.pos = np.zeros(n * CELL * 2, np.float32)
+        self.col = np.zeros(n * CELL * 4, np.uint8)
+        self.fails = 0
+
+    def _args(self):
+        return [_ptr(self.graph_trivial), _ptr(self.graph), _ptr(self.ec_cells), _ptr(self.diag_cells),
+                _ptr(self.ec), _ptr(self.diag), _ptr(self.pos), _ptr(self.col)]
+
+
+def frame(bgr, w, h, ws, subdivide=True, tr=(48, 7, 6), graph_in=None) -> Frame:
+    """Run the oracle's whole path on a reference-layout BGR buffer."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    f = Frame(w, h)
+    gi = None if graph_in is None else np.ascontiguousarray(graph_in, np.uint8)
+    f.fails = lib().orc_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), tr[0], tr[1], tr[2], _ptr(gi), *f._args())
+    return f
+
+
+def yuv_word(b0, b1, b2) -> int:
+    return int(lib().orc_yuv_word(b0, b1, b2))
+
+
+def graph(bgr, w, h, ws, tr=(48, 7, 6)):
+    """Similarity graph, then trivial and heuristic resolution: returns
+    (raw, after_trivial, resolved)."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    raw = np.zeros(w * h, np.uint8)
+    lib().orc_graph(bgr, w, h, ws, tr[0], tr[1], tr[2], raw)
+    triv = raw.copy()
+    lib().orc_trivial(triv, w, h)
+    res = np.zeros(w * h, np.uint8)
+    lib().orc_heuristics(triv, w, h, res)
+    return raw, triv, res
+
+
+def hull_table():
+    counts = np.zeros(4096, np.int32)
+    pts = np.zeros(4096 * 16 * 2, np.int8)
+    lib().orc_hull_table(counts, pts)
+    return counts, pts.reshape(4096, 16, 2)
+
+
+def raster(pos, col, w, h, scale):
+    out = np.zeros(w * scale * h * scale * 4, np.uint8)
+    lib().orc_raster(np.ascontiguousarray(pos, np.float32), np.ascontiguousarray(col, np.uint8), w, h, scale, out)
+    return out.reshape(h * scale, w * scale, 4)
+
+
+def label_cc(graph_resolved, w, h):
+    out = np.zeros(w * h, np.int32)
+    lib().orc_label_cc(np.ascontiguousarray(graph_resolved, np.uint8), w, h, out)
+    return out
+
+
+# ----------------------------------------------------------- reference build
+
+_ref = {}
+
+
+def ref_available(tr_y: int) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libdepix_ref{tr_y}.so"))
+
+
+def ref_lib(tr_y: int):
+    """Host build of the reference's own stage bodies (Y threshold 5 or 48)."""
+    if tr_y not in _ref:
+        L = ctypes.CDLL(os.path.join(REF_DIR, f"libdepix_ref{tr_y}.so"))
+        vp = ctypes.c_void_p
+        L.ref_frame.restype = ctypes.c_int
+        L.ref_frame.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [vp] * 9
+        L.ref_yuv_word.restype = ctypes.c_uint32
+        L.ref_yuv_word.argtypes = [ctypes.c_uint8] * 3
+        _ref[tr_y] = L
+    return _ref[tr_y]
+
+
+def ref_frame(bgr, w, h, ws, subdivide=True, tr_y=48, graph_in=None) -> Frame:
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    f = Frame(w, h)
+    gi = None if graph_in is None else np.ascontiguousarray(graph_in, np.uint8)
+    ref_lib(tr_y).ref_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), _ptr(gi), *f._args())
+    return f
+
+
+def yuv_words(px3: np.ndarray, ref_tr_y: int = 0) -> np.ndarray:
+    """Packed YUV words of an (n, 3) byte array; with ref_tr_y set, computed
+    by the reference's own functions instead of the oracle's."""
+    px3 = np.ascontiguousarray(px3, np.uint8)
+    n = px3.shape[0]
+    out = np.zeros(n, np.uint32)
+    L = ref_lib(ref_tr_y) if ref_tr_y else lib()
+    fn = L.ref_yuv_words if ref_tr_y else L.orc_yuv_words
+    fn.restype = None
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
+    fn(_ptr(px3), n, _ptr(out))
+    return out
