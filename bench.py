@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the depixelization frame path on GB300.
+
+Workload: 256x224 RGBA8 frames from the seeded benchmark-frame generator
+(16 colours, 40 rectangles + 30 ellipses, dark outlines, 5 % dither),
+similarity graph (Y 48, U 7, V 6) -> crossing resolution -> component labels
+-> reshaped cells -> one subdivision round -> triangles -> x4 raster
+(1024x896 RGBA8). A step is one batch of frames through depix_batch.
+
+Prints one JSON line. ``value`` is frames/s of the batched path with inputs
+resident in HBM; ``e2e`` is the same through depix_batch_host with the copies
+from and to pinned host memory inside the timed region; ``plain`` is the
+per-frame path (one launch per stage and frame) with its p50/p99 latency;
+``roofline`` covers the dominant kernel (the fused cells/subdivision/
+triangle/raster kernel); ``cpu_baseline`` is the CPU oracle (a C restatement
+of the reference's per-pixel stage bodies) on this host's cores.
+
+--impl reference times that CPU implementation itself on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "pixel-art-remaster-gpu_gb300")
+ORACLE = os.path.join(REPO, "oracle")
+sys.path.insert(0, PKG)
+
+W, H, SCALE = 256, 224, 4
+METRIC = "frames/s, 256x224 RGBA8 -> x4 (1024x896), batched"
+UNIT = "frames/s"
+DISTINCT = 64
+
+
+def workload_config(batch):
+    return {
+        "workload": "256x224 RGBA8 synthetic frames (16 colours, 40 rects + 30 ellipses, 50% outlined, 5% dither), "
+                    "graph Y48/U7/V6 + trivial + heuristics, component labels, cells + 1 subdivision round + "
+                    "triangles, x4 raster to 1024x896 RGBA8",
+        "frames_per_step": batch,
+        "distinct_frames": DISTINCT,
+        "l2_policy": "inputs larger than L2: %.0f MB read and %.0f MB written per step vs 129 MB L2"
+                     % (batch * W * H * 5 / 1e6, batch * W * H * (SCALE * SCALE * 4 + 4) / 1e6),
+        "parallelism": "replicas",
+    }
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=1024, help="frames per step")
+    ap.add_argument("--plain-frames", type=int, default=300)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="default: max(3, steps // 20)")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU-baseline sample (default 4 x cores)")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def make_frames(n_distinct):
+    import numpy as np
+    from depix import synth
+    return np.stack([synth.frame(seed) for seed in range(n_distinct)])
+
+
+# ------------------------------------------------------------- CPU baseline
+
+
+def cpu_path_frame(img):
+    """The whole path on one frame through the CPU oracle."""
+    import oracle as O
+    from depix import synth
+    bgr, ws = synth.rgba_to_bgr(img)
+    f = O.frame(bgr, W, H, ws, 1, (48, 7, 6))
+    O.label_cc(f.graph, W, H)
+    O.raster(f.pos, f.col, W, H, SCALE)
+
+
+def cpu_run(frames, n_frames, threads):
+    """frames/s of the CPU oracle over n_frames frames on `threads` threads
+    (the C calls release the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda k: cpu_path_frame(frames[k % len(frames)]), range(n_frames)))
+    return n_frames / (time.perf_counter() - t0)
+
+
+def cpu_setup():
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+    O.build()
+    return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- our arm
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per frame of the raster kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "k_raster_256x224_x4.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_frame:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import depix
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    depix.init_device()
+    B = args.batch
+    frames = make_frames(DISTINCT)
+    tiled = np.ascontiguousarray(np.resize(frames, (B, H, W, 4)))
+    in_bytes, out_px = W * H * 4, W * H * SCALE * SCALE
+    d_in = torch.from_numpy(tiled.reshape(-1)).to(dev)
+    d_out = torch.empty(B * out_px * 4, dtype=torch.uint8, device=dev)
+    d_lab = torch.empty(B * W * H, dtype=torch.int32, device=dev)
+    ctx = depix.Context(W * H, B)
+    p = depix.params(48, 7, 6, True, SCALE)
+    ws, hs = [W] * B, [H] * B
+    in_off = [k * in_bytes for k in range(B)]
+    out_off = [k * out_px * 4 for k in range(B)]
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.batch(ws, hs, in_off, out_off, d_in, p, d_out, d_lab, stream=stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ctx.stage_times()  # reset
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ctx.set_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ctx.set_timing(False)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    stages = ctx.stage_times()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    frames_total = B * args.steps * world
+    value = frames_total / (ms / 1e3)
+
+    # roofline of the dominant kernel (raster stage: one kernel per call)
+    r_ms, r_launches, r_calls = stages["raster"]
+    raster_ms = r_ms / max(r_calls, 1)
+    alg_bytes = B * (W * H * 4 + W * H * 1 + out_px * 4)
+    achieved = alg_bytes / (raster_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    tpf = profiled_traffic()
+    roofline = {"kernel": "k_raster (cells + subdivision + ear clip + raster, fused)", "bound": "hbm",
+                "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": (tpf * B if tpf else None),
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": round(raster_ms, 4),
+                "stage_ms_per_step": {k: round(v[0] / max(v[2], 1), 4) for k, v in stages.items()}}
+    launches = sum(v[1] for v in stages.values())
+
+    # end to end through the host-buffer call, copies inside the timed region
+    e2e = None
+    e2e_steps = args.e2e_steps or max(3, args.steps // 20)
+    h_in = torch.from_numpy(tiled.reshape(-1)).pin_memory()
+    h_out = torch.empty(B * out_px * 4, dtype=torch.uint8).pin_memory()
+    h_lab = torch.empty(B * W * H, dtype=torch.int32).pin_memory()
+    for _ in range(2):
+        ctx.batch_host(ws, hs, in_off, out_off, h_in, h_in.numel(), p, h_out, h_out.numel(), h_lab, stream=stream)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.batch_host(ws, hs, in_off, out_off, h_in, h_in.numel(), p, h_out, h_out.numel(), h_lab, stream=stream)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": round(B * e2e_steps * world / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": B * in_bytes,
+           "d2h_bytes_per_step": B * (out_px * 4 + W * H * 4), "steps": e2e_steps}
+    # spot check of the e2e output against the device path
+    assert torch.equal(h_out[: out_px * 4], d_out[: out_px * 4].cpu()), "e2e output differs from device path"
+
+    # plain per-frame path: one launch per stage and frame
+    pf = max(args.plain_frames, 10)
+    ctx1 = depix.Context(W * H, 1)
+    lat = []
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(pf)]
+    for k in range(5):
+        ctx1.frame(d_in[k * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out, None, d_lab, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(pf):
+        a, b = evs[k]
+        a.record(stream)
+        f = k % B
+        ctx1.frame(d_in[f * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out[f * out_px * 4:], None,
+                   d_lab[f * W * H:], stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    lat = sorted(a.elapsed_time(b) for a, b in evs)
+    plain = {"frames_per_s": round(pf / plain_s, 1), "p50_ms_per_frame": round(lat[len(lat) // 2], 4),
+             "p99_ms_per_frame": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4), "frames": pf}
+    ctx1.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cores = cpu_setup()
+        n = args.cpu_sample or 4 * cores
+        cpu_run(frames, min(cores, n), cores)  # warm
+        v = cpu_run(frames, n, cores)
+        cpu = {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{n} frames of the same workload through the CPU oracle (oracle/depix_oracle.c: graph, "
+                         f"resolution, cells, subdivision, ear clip, VBO fill, labels, x4 raster), {cores} threads"}
+    ctx.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
+                "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+        print(json.dumps(line))
+
+
+# ---------------------------------------------------------- reference arm
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = cpu_setup()
+    frames = make_frames(min(DISTINCT, max(cores, 8)))
+    per_step = cores
+    for _ in range(max(args.warmup, 1)):
+        cpu_run(frames, per_step, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_run(frames, per_step, cores)
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    sample = (f"{per_step} frames per step ({cores} threads, one frame each) through the CPU oracle: "
+              f"oracle/depix_oracle.c restates the reference's per-pixel stage bodies; the reference's own "
+              f"sources are not on this machine, so the restatement stands in for them")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded generator)", "config": workload_config(per_step),
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    if rank == 0 or world == 1:
+        import build as depix_build
+        depix_build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

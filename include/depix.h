@@ -1,0 +1,232 @@
+/*
+ * depix.h -- C ABI of the GB300 depixelization library (libdepix.so).
+ *
+ * The library implements the reference's frame path (kernel.cu:286-526 of
+ * marcoc2/pixel-art-remaster-gpu): similarity graph, crossing resolution,
+ * reshaped cells, corner-cutting subdivision, ear-clip triangulation, the
+ * "mapped buffer" VBO output, plus a headless rasterizer that replaces the
+ * OpenGL draw and a connected-component labelling stage.
+ *
+ * Conventions (all entry points):
+ *  - every function returns a depix_status; nothing calls exit();
+ *  - pointers named d_* are device pointers, h_* host pointers; the caller
+ *    owns all memory passed in;
+ *  - work is enqueued on the given stream and the call returns without
+ *    synchronising, except where a function says otherwise;
+ *  - images are rows of pixels with row 0 at the bottom (the y-up order the
+ *    reference works in after its loader flips rows, Image.cpp:21-38);
+ *  - node byte bit e set means "similar to the neighbour in direction e":
+ *        bit  0      1      2      3      4      5       6      7
+ *        (di,dj) (-1,+1) (0,+1) (+1,+1) (-1,0) (+1,0) (-1,-1) (0,-1) (+1,-1)
+ *    (graph_functions.cu:162-235 of the reference).
+ */
+#ifndef DEPIX_H
+#define DEPIX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* depix_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+typedef enum depix_status {
+    DEPIX_OK = 0,
+    DEPIX_ERR_INVALID_ARG = 1, /* bad size, stride, scale or NULL pointer */
+    DEPIX_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+    DEPIX_ERR_ALLOC = 3,       /* device or host allocation failed */
+    DEPIX_ERR_TOO_LARGE = 4,   /* request exceeds a context's or buffer's capacity */
+    DEPIX_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    DEPIX_ERR_CAPTURING = 6,   /* one-time set-up was needed while the stream was being captured */
+    DEPIX_ERR_STATE = 7        /* a device-side consistency check failed */
+} depix_status;
+
+/* Pixel layout of an input image. */
+typedef enum depix_layout {
+    /* the reference's layout: 3 bytes per pixel, B,G,R order, rows
+     * `widthstep` bytes apart (Image.cpp:42-48) */
+    DEPIX_LAYOUT_BGR = 0,
+    /* 4 bytes per pixel R,G,B,A (alpha ignored), rows `widthstep` bytes
+     * apart; handled as the BGR image the reference would have loaded, with
+     * a 4-byte-aligned row stride and zero row padding */
+    DEPIX_LAYOUT_RGBA = 1
+} depix_layout;
+
+typedef struct depix_params {
+    /* similarity thresholds in units of the packed Y/U/V byte fields
+     * (graph_functions.cu:11-19): defaults Y 48, U 7, V 6; the reference's
+     * active build uses Y 5 */
+    int tr_y, tr_u, tr_v;
+    int subdivide; /* run the corner-cutting stage (simpleVBO.cpp:41 default off) */
+    int scale;     /* raster scale factor, 1..64 */
+} depix_params;
+
+void depix_default_params(depix_params* p);
+const char* depix_status_string(depix_status s);
+/* Last CUDA error text seen by this thread ("" if none). */
+const char* depix_last_error(void);
+
+/* One-time per-device set-up (builds the 4096-entry cell-pattern tables on
+ * the current device). Every entry point does it on first use on a device;
+ * call it once before capturing any stream into a CUDA graph. */
+depix_status depix_init_device(void);
+
+/* ---------------------------------------------------------------------
+ * Stage entry points: each mirrors one reference kernel, on device memory.
+ * --------------------------------------------------------------------- */
+
+/* Similarity graph (graph_Kernel, kernel.cu:140-159). With fuse_trivial != 0
+ * the trivial crossing removal (trivial_cross_Kernel, kernel.cu:162-177) is
+ * applied in the same pass. d_graph: w*h bytes. */
+depix_status depix_graph(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                         const depix_params* p, int fuse_trivial, uint8_t* d_graph, depix_stream s);
+
+/* Trivial crossing removal in place (trivial_cross_Kernel, kernel.cu:162-177). */
+depix_status depix_resolve_trivial(uint8_t* d_graph, int w, int h, depix_stream s);
+
+/* Heuristic crossing resolution (ambiguous_cross_Kernel, kernel.cu:180-189):
+ * reads the snapshot d_snapshot (the graph after trivial removal), writes the
+ * resolved graph to d_out. The two buffers must not overlap. */
+depix_status depix_resolve_heuristics(const uint8_t* d_snapshot, int w, int h, uint8_t* d_out, depix_stream s);
+
+/* Reshaped cells (cells_Kernel, kernel.cu:192-213) in the reference's
+ * 45-slot layout: d_diagram gets w*h*45 (x,y) float pairs, local cell
+ * coordinates, count+1 points per cell (the last repeats the first), the
+ * other slots zero; d_edge_count gets the vertex count. */
+depix_status depix_cells(const uint8_t* d_graph, int w, int h, float* d_diagram, int* d_edge_count, depix_stream s);
+
+/* One corner-cutting round (subdivision_Kernel, kernel.cu:216-261): reads
+ * the cell snapshot (d_diagram_snap / d_edge_count_snap, as written by
+ * depix_cells), writes new polygons into d_diagram / d_edge_count; interior
+ * nodes (byte 90) are left untouched, as in the reference. */
+depix_status depix_subdivide(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                             const uint8_t* d_graph, const float* d_diagram_snap, const int* d_edge_count_snap,
+                             float* d_diagram, int* d_edge_count, depix_stream s);
+
+/* Ear-clip triangulation in place (triangulate_Kernel, kernel.cu:264-282):
+ * each cell's first 3*(count-2) slots become triangle corners plus the
+ * cell's (i, j) offset; the remaining slots get (-100,-100). */
+depix_status depix_triangulate(float* d_diagram, const int* d_edge_count, int w, int h, depix_stream s);
+
+/* Mapped-buffer output (position_kernel + color_kernel, kernel.cu:67-137):
+ * d_pos w*h*45 float pairs (unused slots (-100,-100)), d_col w*h*45 RGBA8
+ * (the pixel's R,G,B and alpha 255). Either may be NULL. */
+depix_status depix_emit_vbo(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                            const float* d_diagram, const int* d_edge_count, float* d_pos, uint8_t* d_col,
+                            depix_stream s);
+
+/* Connected components of a resolved graph over its set bits: every node
+ * gets the minimum linear index of its component. d_labels: w*h int32.
+ * (New stage: the reference has only an unbuilt sequential border walk,
+ * cc_functions.cu:348-503.) */
+depix_status depix_label_components(const uint8_t* d_graph, int w, int h, int32_t* d_labels, depix_stream s);
+
+/* Headless raster of a resolved graph (replaces glDrawArrays over the VBO,
+ * simpleVBO.cpp:236-285): rebuilds every cell's (optionally subdivided,
+ * p->subdivide) triangles and writes a (w*scale) x (h*scale) RGBA8 image,
+ * row 0 at the bottom, rows (w*scale*4) bytes apart. Coverage contract:
+ * output pixel (X,Y) samples (X+0.5, Y+0.5); a triangle covers it when its
+ * edge functions are > 0, or == 0 on a top or left edge; the latest triangle
+ * in VBO order wins; uncovered samples are (0,0,0,255). */
+depix_status depix_raster(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                          const uint8_t* d_graph, const depix_params* p, uint8_t* d_out, depix_stream s);
+
+/* Diagnostics. The packed Y/U/V word the graph stage compares (RGBtoYUV,
+ * graph_functions.cu:80-131) for n pixels of 3 bytes in the reference's
+ * memory order (d_px3: 3n bytes, d_words: n uint32). */
+depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, depix_stream s);
+
+/* Copies the per-device cell-pattern tables to host arrays of 4096 entries
+ * each: hull (count in bits 0-3, then 8 vertices of 6 bits: x+1 | (y+1)<<3
+ * in quarter cells) and its ear clip (3 bits per corner index). Synchronous. */
+depix_status depix_pattern_tables(uint64_t* h_hull, uint64_t* h_tri);
+
+/* ---------------------------------------------------------------------
+ * Frame path with a context that owns its scratch (no allocation per call).
+ * --------------------------------------------------------------------- */
+
+typedef struct depix_context depix_context;
+
+/* Scratch for frames of up to max_pixels pixels each and up to max_frames
+ * frames per batch call. */
+depix_status depix_context_create(depix_context** ctx, size_t max_pixels, int max_frames);
+depix_status depix_context_destroy(depix_context* ctx);
+
+/* Whole path on one device-resident frame: graph + trivial -> heuristics ->
+ * [labels] -> raster. d_graph_out (w*h) and d_labels (w*h int32) may be NULL. */
+depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h, int widthstep,
+                         depix_layout layout, const depix_params* p, uint8_t* d_out, uint8_t* d_graph_out,
+                         int32_t* d_labels, depix_stream s);
+
+/* A batch of frames, each with its own size. Frame k reads its image at
+ * d_img + in_offset[k] (RGBA8, rows w[k]*4 bytes apart) and writes its raster
+ * at d_out + out_offset[k] (rows w[k]*scale*4 bytes apart); offsets are in
+ * bytes and must be multiples of 16. With d_labels set, frame k's component
+ * labels go to d_labels + (w[0]*h[0] + ... + w[k-1]*h[k-1]). Host arrays w,
+ * h, in_offset, out_offset have n entries. Frames of one size at a constant
+ * stride go through one launch per stage for the whole batch. */
+depix_status depix_batch(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                         const uint64_t* out_offset, const uint8_t* d_img, const depix_params* p, uint8_t* d_out,
+                         int32_t* d_labels, depix_stream s);
+
+/* depix_batch on HOST buffers: copies h_img (in_bytes) to the device, runs
+ * the batch, copies the rasters back to h_out (out_bytes) and, when h_labels
+ * is set, the labels. Device staging is owned by the context (allocated on
+ * the first call that needs more). Synchronous. Pinned host memory gives the
+ * full copy bandwidth. */
+depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                              const uint64_t* out_offset, const uint8_t* h_img, size_t in_bytes,
+                              const depix_params* p, uint8_t* h_out, size_t out_bytes, int32_t* h_labels,
+                              depix_stream s);
+
+/* Per-stage device timing of a context's frame and batch calls. */
+enum {
+    DEPIX_STAGE_GRAPH = 0,      /* similarity graph + trivial removal */
+    DEPIX_STAGE_HEURISTICS = 1, /* heuristic crossing resolution */
+    DEPIX_STAGE_LABELS = 2,     /* component labels */
+    DEPIX_STAGE_RASTER = 3,     /* cells, subdivision, triangles, raster */
+    DEPIX_STAGE_COUNT = 4
+};
+/* Turns CUDA-event timing of every stage launch on or off (off by default). */
+depix_status depix_context_set_timing(depix_context* ctx, int enable);
+/* Accumulated device milliseconds, kernel launches and stage calls per stage
+ * since the last reset (arrays of DEPIX_STAGE_COUNT; any may be NULL), then
+ * resets. Waits for the recorded events. */
+depix_status depix_context_stage_times(depix_context* ctx, double* ms, long long* launches, long long* calls);
+
+/* ---------------------------------------------------------------------
+ * Drop-in replacement of the reference's frame driver.
+ * --------------------------------------------------------------------- */
+
+typedef struct depix_point { float x, y; } depix_point; /* Point, point.cu:2-11 */
+
+/* Same arguments and layout as launch_kernel (kernel.cu:286-288), plus the
+ * thresholds: pos / colorPos are caller-owned DEVICE buffers of w*h*45
+ * float2 / uchar4; img_data is a host BGR image (stride img_widthstep);
+ * edge_count_h (w*h int) and graph_h (w*h bytes) are host outputs; time is
+ * unused; p NULL means the reference build's thresholds (Y 5, U 7, V 6) and
+ * p->subdivide / p->scale are ignored. Returns a malloc'd host array of
+ * w*h*45 points (the triangulated cells, unused slots (-100,-100)) that the
+ * caller frees, or NULL on error (see depix_last_error). Synchronous; scratch
+ * is kept per process between calls and guarded by a lock. */
+depix_point* depix_launch_kernel_compat(void* pos, void* colorPos, float time, char* img_data, int img_width,
+                                        int img_height, int img_widthstep, int* edge_count_h, char* graph_h,
+                                        int subdivide, const depix_params* p);
+
+#ifdef __cplusplus
+#define DEPIX_BOOL bool
+#else
+#define DEPIX_BOOL _Bool
+#endif
+/* The reference's own symbol (kernel.cu:286), forwarding to the function
+ * above with the reference build's thresholds. */
+depix_point* launch_kernel(void* pos, void* colorPos, float time, char* img_data, int img_width, int img_height,
+                           int img_widthstep, int* edge_count_h, char* graph_h, DEPIX_BOOL subdivide);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEPIX_H */

@@ -1,0 +1,724 @@
+// depix_api.cu -- host side of the C ABI: argument checks, per-device
+// set-up, the frame/batch drivers and the drop-in launch_kernel.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "depix_internal.h"
+
+using namespace depix;
+
+namespace {
+
+thread_local std::string t_last_error;
+
+depix_status cuda_fail(cudaError_t e, const char* where)
+{
+    t_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return DEPIX_ERR_CUDA;
+}
+
+depix_status arg_fail(const char* what)
+{
+    t_last_error = what;
+    return DEPIX_ERR_INVALID_ARG;
+}
+
+#define DEPIX_CK(call)                                                  \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);             \
+    } while (0)
+
+#define DEPIX_TRY(call)                                                 \
+    do {                                                                \
+        depix_status st_ = (call);                                      \
+        if (st_ != DEPIX_OK) return st_;                                \
+    } while (0)
+
+std::mutex g_init_mu;
+std::vector<char> g_init_done;
+
+// Builds the cell-pattern tables on the current device once. Uses a private
+// stream that it synchronises, so the tables are complete before any later
+// work on any stream.
+depix_status ensure_tables(cudaStream_t user)
+{
+    int dev = 0;
+    DEPIX_CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (dev < (int)g_init_done.size() && g_init_done[dev]) return DEPIX_OK;
+    if (user) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        DEPIX_CK(cudaStreamIsCapturing(user, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+            t_last_error = "first use on this device inside a stream capture: call depix_init_device() first";
+            return DEPIX_ERR_CAPTURING;
+        }
+    }
+    cudaStream_t s;
+    DEPIX_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaError_t e = init_tables(s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) return cuda_fail(e, "init_tables");
+    if (dev >= (int)g_init_done.size()) g_init_done.resize(dev + 1, 0);
+    g_init_done[dev] = 1;
+    return DEPIX_OK;
+}
+
+depix_status check_size(int w, int h)
+{
+    if (w < 1 || h < 1) return arg_fail("width and height must be >= 1");
+    if ((long long)w * h > (1LL << 30)) return arg_fail("frame larger than 2^30 pixels");
+    return DEPIX_OK;
+}
+
+depix_status check_image(const uint8_t* img, int w, int h, int ws, int layout)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!img) return arg_fail("image pointer is NULL");
+    if (layout == DEPIX_LAYOUT_BGR) {
+        if (ws < 3 * w) return arg_fail("BGR widthstep must be >= 3*width");
+    } else if (layout == DEPIX_LAYOUT_RGBA) {
+        if (ws < 4 * w || (ws & 3) || (reinterpret_cast<uintptr_t>(img) & 3))
+            return arg_fail("RGBA widthstep must be >= 4*width, rows and base 4-byte aligned");
+    } else {
+        return arg_fail("unknown layout");
+    }
+    return DEPIX_OK;
+}
+
+depix_status check_params(const depix_params* p)
+{
+    if (!p) return arg_fail("params pointer is NULL");
+    if (p->scale < 1 || p->scale > 64) return arg_fail("scale must be in 1..64");
+    if (p->tr_y < 0 || p->tr_u < 0 || p->tr_v < 0) return arg_fail("thresholds must be >= 0");
+    return DEPIX_OK;
+}
+
+// the raster addresses samples in 1/256 output pixel with 32-bit integers
+constexpr long long kMaxOutSide = 1LL << 22;
+
+depix_status check_out_size(int w, int h, const depix_params* p)
+{
+    if ((long long)w * p->scale > kMaxOutSide || (long long)h * p->scale > kMaxOutSide)
+        return arg_fail("output side beyond 2^22 pixels");
+    return DEPIX_OK;
+}
+
+inline cudaStream_t S(depix_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+void depix_default_params(depix_params* p)
+{
+    if (!p) return;
+    p->tr_y = 48;
+    p->tr_u = 7;
+    p->tr_v = 6;
+    p->subdivide = 1;
+    p->scale = 4;
+}
+
+const char* depix_status_string(depix_status s)
+{
+    switch (s) {
+    case DEPIX_OK: return "ok";
+    case DEPIX_ERR_INVALID_ARG: return "invalid argument";
+    case DEPIX_ERR_CUDA: return "CUDA error";
+    case DEPIX_ERR_ALLOC: return "allocation failed";
+    case DEPIX_ERR_TOO_LARGE: return "request exceeds capacity";
+    case DEPIX_ERR_TIMEOUT: return "device wait timed out";
+    case DEPIX_ERR_CAPTURING: return "set-up needed during stream capture";
+    case DEPIX_ERR_STATE: return "device consistency check failed";
+    }
+    return "unknown status";
+}
+
+const char* depix_last_error(void) { return t_last_error.c_str(); }
+
+depix_status depix_init_device(void) { return ensure_tables(nullptr); }
+
+depix_status depix_graph(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                         const depix_params* p, int fuse_trivial, uint8_t* d_graph, depix_stream s)
+{
+    DEPIX_TRY(check_image(d_img, w, h, widthstep, layout));
+    DEPIX_TRY(check_params(p));
+    if (!d_graph) return arg_fail("graph pointer is NULL");
+    FrameBatch b{d_img, 0, d_graph, 0, w, h, widthstep, (int)layout};
+    DEPIX_CK(launch_graph(b, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), fuse_trivial != 0, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_resolve_trivial(uint8_t* d_graph, int w, int h, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_graph) return arg_fail("graph pointer is NULL");
+    DEPIX_CK(launch_trivial(d_graph, w, h, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_resolve_heuristics(const uint8_t* d_snapshot, int w, int h, uint8_t* d_out, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_snapshot || !d_out) return arg_fail("graph pointer is NULL");
+    if (d_snapshot == d_out) return arg_fail("snapshot and output must be distinct buffers");
+    GraphBatch b{d_snapshot, d_out, 0, w, h};
+    DEPIX_CK(launch_heuristics(b, 1, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_cells(const uint8_t* d_graph, int w, int h, float* d_diagram, int* d_edge_count, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_graph || !d_diagram || !d_edge_count) return arg_fail("NULL pointer");
+    DEPIX_TRY(ensure_tables(S(s)));
+    DEPIX_CK(launch_cells(d_graph, w, h, d_diagram, d_edge_count, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_subdivide(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                             const uint8_t* d_graph, const float* d_diagram_snap, const int* d_edge_count_snap,
+                             float* d_diagram, int* d_edge_count, depix_stream s)
+{
+    DEPIX_TRY(check_image(d_img, w, h, widthstep, layout));
+    if (!d_graph || !d_diagram_snap || !d_edge_count_snap || !d_diagram || !d_edge_count)
+        return arg_fail("NULL pointer");
+    DEPIX_CK(launch_subdivide(d_img, w, h, widthstep, layout, d_graph, d_diagram_snap, d_edge_count_snap, d_diagram,
+                              d_edge_count, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_triangulate(float* d_diagram, const int* d_edge_count, int w, int h, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_diagram || !d_edge_count) return arg_fail("NULL pointer");
+    DEPIX_CK(launch_triangulate(d_diagram, d_edge_count, w, h, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_emit_vbo(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                            const float* d_diagram, const int* d_edge_count, float* d_pos, uint8_t* d_col,
+                            depix_stream s)
+{
+    DEPIX_TRY(check_image(d_img, w, h, widthstep, layout));
+    if (!d_diagram || !d_edge_count) return arg_fail("NULL pointer");
+    DEPIX_CK(launch_emit(d_img, w, h, widthstep, layout, d_diagram, d_edge_count, d_pos, d_col, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_label_components(const uint8_t* d_graph, int w, int h, int32_t* d_labels, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_graph || !d_labels) return arg_fail("NULL pointer");
+    DEPIX_CK(launch_labels(d_graph, d_labels, w, h, 1, 0, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, depix_stream s)
+{
+    if (n && (!d_px3 || !d_words)) return arg_fail("NULL pointer");
+    DEPIX_CK(launch_yuv_words(d_px3, n, d_words, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_pattern_tables(uint64_t* h_hull, uint64_t* h_tri)
+{
+    if (!h_hull || !h_tri) return arg_fail("NULL pointer");
+    DEPIX_TRY(ensure_tables(nullptr));
+    DEPIX_CK(copy_tables(h_hull, h_tri));
+    return DEPIX_OK;
+}
+
+depix_status depix_raster(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                          const uint8_t* d_graph, const depix_params* p, uint8_t* d_out, depix_stream s)
+{
+    DEPIX_TRY(check_image(d_img, w, h, widthstep, layout));
+    DEPIX_TRY(check_params(p));
+    if (!d_graph || !d_out) return arg_fail("NULL pointer");
+    DEPIX_TRY(check_out_size(w, h, p));
+    DEPIX_TRY(ensure_tables(S(s)));
+    RasterBatch b{d_img, 0, d_graph, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};
+    DEPIX_CK(launch_raster(b, 1, S(s)));
+    return DEPIX_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ context
+
+struct depix_context {
+    int device = 0;
+    size_t max_pixels = 0;
+    int max_frames = 0;
+    uint8_t* graph_a = nullptr; // after graph + trivial, max_frames slots of max_pixels
+    uint8_t* graph_b = nullptr; // resolved
+    // device staging of the host-buffer batch call
+    uint8_t* stage_in = nullptr;
+    size_t stage_in_bytes = 0;
+    uint8_t* stage_out = nullptr;
+    size_t stage_out_bytes = 0;
+    int32_t* stage_labels = nullptr;
+    size_t stage_label_count = 0;
+    // per-stage event timing
+    bool timing = false;
+    struct Mark {
+        int stage;
+        int launches;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> spare;
+    double ms[DEPIX_STAGE_COUNT] = {0, 0, 0, 0};
+    long long launches[DEPIX_STAGE_COUNT] = {0, 0, 0, 0};
+    long long calls[DEPIX_STAGE_COUNT] = {0, 0, 0, 0};
+
+    cudaEvent_t take_event()
+    {
+        if (!spare.empty()) {
+            cudaEvent_t e = spare.back();
+            spare.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+
+namespace {
+
+// Brackets one stage's launches with events when the context is timing.
+struct StageTimer {
+    depix_context* c;
+    int stage, launches;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    StageTimer(depix_context* c_, int stage_, int launches_, cudaStream_t s_)
+        : c(c_), stage(stage_), launches(launches_), s(s_)
+    {
+        if (c->timing) {
+            a = c->take_event();
+            cudaEventRecord(a, s);
+        }
+    }
+    ~StageTimer()
+    {
+        if (!c->timing || !a) return;
+        cudaEvent_t b = c->take_event();
+        cudaEventRecord(b, s);
+        c->marks.push_back({stage, launches, a, b});
+    }
+};
+
+depix_status ensure_staging(depix_context* c, size_t in_bytes, size_t out_bytes, size_t labels)
+{
+    if (in_bytes > c->stage_in_bytes) {
+        cudaFree(c->stage_in);
+        c->stage_in = nullptr;
+        c->stage_in_bytes = 0;
+        if (cudaMalloc(&c->stage_in, in_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            t_last_error = "cudaMalloc of input staging failed";
+            return DEPIX_ERR_ALLOC;
+        }
+        c->stage_in_bytes = in_bytes;
+    }
+    if (out_bytes > c->stage_out_bytes) {
+        cudaFree(c->stage_out);
+        c->stage_out = nullptr;
+        c->stage_out_bytes = 0;
+        if (cudaMalloc(&c->stage_out, out_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            t_last_error = "cudaMalloc of output staging failed";
+            return DEPIX_ERR_ALLOC;
+        }
+        c->stage_out_bytes = out_bytes;
+    }
+    if (labels > c->stage_label_count) {
+        cudaFree(c->stage_labels);
+        c->stage_labels = nullptr;
+        c->stage_label_count = 0;
+        if (cudaMalloc(&c->stage_labels, labels * sizeof(int32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            t_last_error = "cudaMalloc of label staging failed";
+            return DEPIX_ERR_ALLOC;
+        }
+        c->stage_label_count = labels;
+    }
+    return DEPIX_OK;
+}
+
+struct BatchShape {
+    bool uniform = true, strided = true;
+    size_t total_pixels = 0;
+};
+
+depix_status check_batch(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                         const uint64_t* out_offset, BatchShape& shape)
+{
+    if (n > ctx->max_frames) {
+        t_last_error = "more frames than the context capacity";
+        return DEPIX_ERR_TOO_LARGE;
+    }
+    for (int k = 0; k < n; k++) {
+        DEPIX_TRY(check_size(w[k], h[k]));
+        if ((size_t)w[k] * h[k] > ctx->max_pixels) {
+            t_last_error = "frame larger than the context capacity";
+            return DEPIX_ERR_TOO_LARGE;
+        }
+        if ((in_offset[k] & 15) || (out_offset[k] & 15)) return arg_fail("offsets must be multiples of 16");
+        if (w[k] != w[0] || h[k] != h[0]) shape.uniform = false;
+        shape.total_pixels += (size_t)w[k] * h[k];
+    }
+    if (n > 1) {
+        uint64_t is = in_offset[1] - in_offset[0], os = out_offset[1] - out_offset[0];
+        for (int k = 1; k < n; k++)
+            if (in_offset[k] - in_offset[k - 1] != is || out_offset[k] - out_offset[k - 1] != os) shape.strided = false;
+    }
+    return DEPIX_OK;
+}
+
+depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                       const uint64_t* out_offset, const uint8_t* d_img, const depix_params* p, uint8_t* d_out,
+                       int32_t* d_labels, const BatchShape& shape, cudaStream_t s)
+{
+    const uint32_t thr = pack_thresholds(p->tr_y, p->tr_u, p->tr_v);
+    if (shape.uniform && shape.strided) {
+        // equal sizes at equal strides: one launch per stage for the batch
+        size_t px = (size_t)w[0] * h[0];
+        uint64_t is = n > 1 ? in_offset[1] - in_offset[0] : 0, os = n > 1 ? out_offset[1] - out_offset[0] : 0;
+        const uint8_t* img0 = d_img + in_offset[0];
+        {
+            StageTimer t(ctx, DEPIX_STAGE_GRAPH, 1, s);
+            FrameBatch gb{img0, (size_t)is, ctx->graph_a, px, w[0], h[0], 4 * w[0], DEPIX_LAYOUT_RGBA};
+            DEPIX_CK(launch_graph(gb, n, thr, true, s));
+        }
+        {
+            StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
+            GraphBatch hb{ctx->graph_a, ctx->graph_b, px, w[0], h[0]};
+            DEPIX_CK(launch_heuristics(hb, n, s));
+        }
+        if (d_labels) {
+            StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
+            DEPIX_CK(launch_labels(ctx->graph_b, d_labels, w[0], h[0], n, px, s));
+        }
+        {
+            StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
+            RasterBatch rb{img0, (size_t)is, ctx->graph_b, px, d_out + out_offset[0], (size_t)os, w[0], h[0],
+                           4 * w[0], DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
+            DEPIX_CK(launch_raster(rb, n, s));
+        }
+        return DEPIX_OK;
+    }
+    // uneven frames: one launch per stage and frame
+    size_t goff = 0, loff = 0;
+    for (int k = 0; k < n; k++) {
+        const uint8_t* img = d_img + in_offset[k];
+        {
+            StageTimer t(ctx, DEPIX_STAGE_GRAPH, 1, s);
+            FrameBatch gb{img, 0, ctx->graph_a + goff, 0, w[k], h[k], 4 * w[k], DEPIX_LAYOUT_RGBA};
+            DEPIX_CK(launch_graph(gb, 1, thr, true, s));
+        }
+        {
+            StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
+            GraphBatch hb{ctx->graph_a + goff, ctx->graph_b + goff, 0, w[k], h[k]};
+            DEPIX_CK(launch_heuristics(hb, 1, s));
+        }
+        if (d_labels) {
+            StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
+            DEPIX_CK(launch_labels(ctx->graph_b + goff, d_labels + loff, w[k], h[k], 1, 0, s));
+        }
+        {
+            StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
+            RasterBatch rb{img, 0, ctx->graph_b + goff, 0, d_out + out_offset[k], 0, w[k], h[k], 4 * w[k],
+                           DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
+            DEPIX_CK(launch_raster(rb, 1, s));
+        }
+        goff += ctx->max_pixels;
+        loff += (size_t)w[k] * h[k];
+    }
+    return DEPIX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+depix_status depix_context_create(depix_context** out, size_t max_pixels, int max_frames)
+{
+    if (!out) return arg_fail("NULL context pointer");
+    *out = nullptr;
+    if (max_pixels < 1 || max_frames < 1) return arg_fail("capacity must be >= 1");
+    DEPIX_TRY(ensure_tables(nullptr));
+    depix_context* c = new (std::nothrow) depix_context();
+    if (!c) return DEPIX_ERR_ALLOC;
+    DEPIX_CK(cudaGetDevice(&c->device));
+    c->max_pixels = max_pixels;
+    c->max_frames = max_frames;
+    size_t bytes = max_pixels * (size_t)max_frames;
+    if (cudaMalloc(&c->graph_a, bytes) != cudaSuccess || cudaMalloc(&c->graph_b, bytes) != cudaSuccess) {
+        cudaFree(c->graph_a);
+        delete c;
+        t_last_error = "cudaMalloc of context scratch failed";
+        cudaGetLastError();
+        return DEPIX_ERR_ALLOC;
+    }
+    *out = c;
+    return DEPIX_OK;
+}
+
+depix_status depix_context_destroy(depix_context* c)
+{
+    if (!c) return DEPIX_OK;
+    cudaFree(c->graph_a);
+    cudaFree(c->graph_b);
+    cudaFree(c->stage_in);
+    cudaFree(c->stage_out);
+    cudaFree(c->stage_labels);
+    for (auto& m : c->marks) {
+        cudaEventDestroy(m.a);
+        cudaEventDestroy(m.b);
+    }
+    for (auto e : c->spare) cudaEventDestroy(e);
+    delete c;
+    return DEPIX_OK;
+}
+
+depix_status depix_context_set_timing(depix_context* c, int enable)
+{
+    if (!c) return arg_fail("NULL context");
+    c->timing = enable != 0;
+    return DEPIX_OK;
+}
+
+depix_status depix_context_stage_times(depix_context* c, double* ms, long long* launches, long long* calls)
+{
+    if (!c) return arg_fail("NULL context");
+    for (auto& m : c->marks) {
+        DEPIX_CK(cudaEventSynchronize(m.b));
+        float t = 0;
+        DEPIX_CK(cudaEventElapsedTime(&t, m.a, m.b));
+        c->ms[m.stage] += t;
+        c->launches[m.stage] += m.launches;
+        c->calls[m.stage] += 1;
+        c->spare.push_back(m.a);
+        c->spare.push_back(m.b);
+    }
+    c->marks.clear();
+    for (int k = 0; k < DEPIX_STAGE_COUNT; k++) {
+        if (ms) ms[k] = c->ms[k];
+        if (launches) launches[k] = c->launches[k];
+        if (calls) calls[k] = c->calls[k];
+        c->ms[k] = 0;
+        c->launches[k] = 0;
+        c->calls[k] = 0;
+    }
+    return DEPIX_OK;
+}
+
+depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
+                         const depix_params* p, uint8_t* d_out, uint8_t* d_graph_out, int32_t* d_labels,
+                         depix_stream s_)
+{
+    if (!ctx) return arg_fail("NULL context");
+    DEPIX_TRY(check_image(d_img, w, h, widthstep, layout));
+    DEPIX_TRY(check_params(p));
+    if ((size_t)w * h > ctx->max_pixels) {
+        t_last_error = "frame larger than the context capacity";
+        return DEPIX_ERR_TOO_LARGE;
+    }
+    if (d_out) DEPIX_TRY(check_out_size(w, h, p));
+    cudaStream_t s = S(s_);
+    uint8_t* resolved = d_graph_out ? d_graph_out : ctx->graph_b;
+    {
+        StageTimer t(ctx, DEPIX_STAGE_GRAPH, 1, s);
+        FrameBatch gb{d_img, 0, ctx->graph_a, 0, w, h, widthstep, (int)layout};
+        DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+    }
+    {
+        StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
+        GraphBatch hb{ctx->graph_a, resolved, 0, w, h};
+        DEPIX_CK(launch_heuristics(hb, 1, s));
+    }
+    if (d_labels) {
+        StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
+        DEPIX_CK(launch_labels(resolved, d_labels, w, h, 1, 0, s));
+    }
+    if (d_out) {
+        StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
+        RasterBatch rb{d_img, 0, resolved, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};
+        DEPIX_CK(launch_raster(rb, 1, s));
+    }
+    return DEPIX_OK;
+}
+
+depix_status depix_batch(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                         const uint64_t* out_offset, const uint8_t* d_img, const depix_params* p, uint8_t* d_out,
+                         int32_t* d_labels, depix_stream s)
+{
+    if (!ctx) return arg_fail("NULL context");
+    if (n < 0 || (n > 0 && (!w || !h || !in_offset || !out_offset || !d_img || !d_out)))
+        return arg_fail("bad batch arguments");
+    DEPIX_TRY(check_params(p));
+    if (n == 0) return DEPIX_OK;
+    BatchShape shape;
+    DEPIX_TRY(check_batch(ctx, n, w, h, in_offset, out_offset, shape));
+    for (int k = 0; k < n; k++) DEPIX_TRY(check_out_size(w[k], h[k], p));
+    return run_batch(ctx, n, w, h, in_offset, out_offset, d_img, p, d_out, d_labels, shape, S(s));
+}
+
+depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                              const uint64_t* out_offset, const uint8_t* h_img, size_t in_bytes,
+                              const depix_params* p, uint8_t* h_out, size_t out_bytes, int32_t* h_labels,
+                              depix_stream s_)
+{
+    if (!ctx) return arg_fail("NULL context");
+    if (n < 0 || (n > 0 && (!w || !h || !in_offset || !out_offset || !h_img || !h_out)))
+        return arg_fail("bad batch arguments");
+    DEPIX_TRY(check_params(p));
+    if (n == 0) return DEPIX_OK;
+    BatchShape shape;
+    DEPIX_TRY(check_batch(ctx, n, w, h, in_offset, out_offset, shape));
+    for (int k = 0; k < n; k++) DEPIX_TRY(check_out_size(w[k], h[k], p));
+    for (int k = 0; k < n; k++) {
+        size_t ib = (size_t)w[k] * h[k] * 4, ob = ib * (size_t)p->scale * p->scale;
+        if (in_offset[k] + ib > in_bytes || out_offset[k] + ob > out_bytes)
+            return arg_fail("a frame lies outside the host buffers");
+    }
+    DEPIX_TRY(ensure_staging(ctx, in_bytes, out_bytes, h_labels ? shape.total_pixels : 0));
+    cudaStream_t s = S(s_);
+    DEPIX_CK(cudaMemcpyAsync(ctx->stage_in, h_img, in_bytes, cudaMemcpyHostToDevice, s));
+    DEPIX_TRY(run_batch(ctx, n, w, h, in_offset, out_offset, ctx->stage_in, p, ctx->stage_out,
+                        h_labels ? ctx->stage_labels : nullptr, shape, s));
+    DEPIX_CK(cudaMemcpyAsync(h_out, ctx->stage_out, out_bytes, cudaMemcpyDeviceToHost, s));
+    if (h_labels)
+        DEPIX_CK(cudaMemcpyAsync(h_labels, ctx->stage_labels, shape.total_pixels * sizeof(int32_t),
+                                 cudaMemcpyDeviceToHost, s));
+    DEPIX_CK(cudaStreamSynchronize(s));
+    return DEPIX_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------ drop-in frame driver
+
+namespace {
+
+struct CompatScratch {
+    size_t img_bytes = 0, pixels = 0;
+    uint8_t* img = nullptr;
+    uint8_t* g0 = nullptr;
+    uint8_t* g1 = nullptr;
+    float* diag = nullptr;
+    float* snap = nullptr;
+    int* ec = nullptr;
+    int* ec_snap = nullptr;
+    void release()
+    {
+        cudaFree(img); cudaFree(g0); cudaFree(g1); cudaFree(diag); cudaFree(snap); cudaFree(ec); cudaFree(ec_snap);
+        *this = CompatScratch();
+    }
+    bool reserve(size_t ib, size_t px)
+    {
+        if (ib <= img_bytes && px <= pixels && img) return true;
+        release();
+        bool ok = cudaMalloc(&img, ib) == cudaSuccess && cudaMalloc(&g0, px) == cudaSuccess &&
+                  cudaMalloc(&g1, px) == cudaSuccess &&
+                  cudaMalloc(&diag, px * kCell * sizeof(float2)) == cudaSuccess &&
+                  cudaMalloc(&snap, px * kCell * sizeof(float2)) == cudaSuccess &&
+                  cudaMalloc(&ec, px * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&ec_snap, px * sizeof(int)) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            release();
+            return false;
+        }
+        img_bytes = ib;
+        pixels = px;
+        return true;
+    }
+};
+
+std::mutex g_compat_mu;
+CompatScratch g_compat;
+
+depix_status compat_run(void* pos, void* colorPos, char* img_data, int w, int h, int ws, int* edge_count_h,
+                        char* graph_h, int subdivide, const depix_params* p, depix_point** result)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!img_data || ws < 3 * w) return arg_fail("bad host image");
+    depix_params ref{5, 7, 6, 0, 1};
+    if (!p) p = &ref;
+    DEPIX_TRY(check_params(p));
+    DEPIX_TRY(ensure_tables(nullptr));
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    size_t px = (size_t)w * h, ib = (size_t)ws * h;
+    if (!g_compat.reserve(ib, px)) {
+        t_last_error = "cudaMalloc of compat scratch failed";
+        return DEPIX_ERR_ALLOC;
+    }
+    CompatScratch& c = g_compat;
+    cudaStream_t s = 0;
+    DEPIX_CK(cudaMemcpyAsync(c.img, img_data, ib, cudaMemcpyHostToDevice, s));
+    FrameBatch gb{c.img, 0, c.g0, 0, w, h, ws, DEPIX_LAYOUT_BGR};
+    DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+    GraphBatch hb{c.g0, c.g1, 0, w, h};
+    DEPIX_CK(launch_heuristics(hb, 1, s));
+    DEPIX_CK(launch_cells(c.g1, w, h, c.diag, c.ec, s));
+    if (subdivide) {
+        DEPIX_CK(cudaMemcpyAsync(c.snap, c.diag, px * kCell * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+        DEPIX_CK(cudaMemcpyAsync(c.ec_snap, c.ec, px * sizeof(int), cudaMemcpyDeviceToDevice, s));
+        DEPIX_CK(launch_subdivide(c.img, w, h, ws, DEPIX_LAYOUT_BGR, c.g1, c.snap, c.ec_snap, c.diag, c.ec, s));
+    }
+    DEPIX_CK(launch_triangulate(c.diag, c.ec, w, h, s));
+    if (pos || colorPos)
+        DEPIX_CK(launch_emit(c.img, w, h, ws, DEPIX_LAYOUT_BGR, c.diag, c.ec, static_cast<float*>(pos),
+                             static_cast<uint8_t*>(colorPos), s));
+    if (edge_count_h) DEPIX_CK(cudaMemcpyAsync(edge_count_h, c.ec, px * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (graph_h) DEPIX_CK(cudaMemcpyAsync(graph_h, c.g1, px, cudaMemcpyDeviceToHost, s));
+    depix_point* out = static_cast<depix_point*>(malloc(px * kCell * sizeof(depix_point)));
+    if (!out) {
+        cudaStreamSynchronize(s);
+        t_last_error = "host malloc failed";
+        return DEPIX_ERR_ALLOC;
+    }
+    cudaError_t e = cudaMemcpyAsync(out, c.diag, px * kCell * sizeof(float2), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        free(out);
+        return cuda_fail(e, "compat frame");
+    }
+    *result = out;
+    return DEPIX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+depix_point* depix_launch_kernel_compat(void* pos, void* colorPos, float, char* img_data, int img_width,
+                                        int img_height, int img_widthstep, int* edge_count_h, char* graph_h,
+                                        int subdivide, const depix_params* p)
+{
+    depix_point* r = nullptr;
+    if (compat_run(pos, colorPos, img_data, img_width, img_height, img_widthstep, edge_count_h, graph_h, subdivide, p,
+                   &r) != DEPIX_OK)
+        return nullptr;
+    return r;
+}
+
+depix_point* launch_kernel(void* pos, void* colorPos, float time, char* img_data, int img_width, int img_height,
+                           int img_widthstep, int* edge_count_h, char* graph_h, bool subdivide)
+{
+    return depix_launch_kernel_compat(pos, colorPos, time, img_data, img_width, img_height, img_widthstep,
+                                      edge_count_h, graph_h, subdivide ? 1 : 0, nullptr);
+}
+
+}  // extern "C"

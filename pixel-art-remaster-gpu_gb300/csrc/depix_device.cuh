@@ -1,0 +1,346 @@
+// depix_device.cuh -- device-side building blocks shared by the kernels.
+//
+// Geometry is carried in exact integers: every coordinate the reference
+// produces is a multiple of 1/64 of a cell (hull points are multiples of
+// 1/4, one corner-cutting round and the neighbour midpoints add three more
+// halvings), and its float and double arithmetic on such values is exact. So
+// the hull, subdivision and ear-clip decisions below, made on integers in
+// 1/64-cell units, are the reference's decisions bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/depix.h"
+
+namespace depix {
+
+constexpr int kCell = 45;    // slots per cell in the VBO layout (kernel.cu:8)
+constexpr int kMaxHull = 8;  // largest reshaped-cell hull over all 4096 patterns
+constexpr int kMaxPoly = 16; // one subdivision round at most doubles the hull
+constexpr int kUnit = 64;    // geometry units per cell
+
+// neighbour offset of node bit e (graph_functions.cu:162-235), j upward
+__host__ __device__ __forceinline__ int dir_di(int e) { return ((0x9224 >> (2 * e)) & 3) - 1; }
+__host__ __device__ __forceinline__ int dir_dj(int e) { return ((0x016A >> (2 * e)) & 3) - 1; }
+__host__ __device__ __forceinline__ int bitof(unsigned v, int k) { return (int)((v >> k) & 1u); }
+
+// ------------------------------------------------------------------ colour
+
+// Packed Y/U/V word of one pixel from its bytes in the reference's memory
+// order (b0 plays "r", b2 plays "b": RGBtoYUV + DATAtoINT,
+// graph_functions.cu:80-131). y is the truncated double 0.299 r + 0.587 g +
+// 0.114 b; off exact multiples of 1/1000 that equals the integer quotient of
+// 299 r + 587 g + 114 b by 1000, so the double evaluation (no contraction) is
+// only needed when the remainder is zero.
+__device__ __forceinline__ uint32_t yuv_word(int r, int g, int b)
+{
+    int s = 299 * r + 587 * g + 114 * b;
+    int y = s / 1000;
+    if (s - y * 1000 == 0) {
+        double t = __dadd_rn(__dmul_rn(0.299, (double)r), __dmul_rn(0.587, (double)g));
+        t = __dadd_rn(t, __dmul_rn(0.114, (double)b));
+        y = __double2int_rz(t);
+    }
+    int u = __float2int_rz(__fmul_rn((float)(b - y), 0.492f));
+    int v = __float2int_rz(__fmul_rn((float)(r - y), 0.877f));
+    return (uint32_t)(y * 65536 + u * 256 + v);
+}
+
+// thresholds packed like a word; a field threshold above 255 can never be exceeded
+__host__ __device__ __forceinline__ uint32_t pack_thresholds(int ty, int tu, int tv)
+{
+    auto c = [](int t) { return (uint32_t)(t < 0 ? 0 : (t > 255 ? 255 : t)); };
+    return (c(ty) << 16) | (c(tu) << 8) | c(tv);
+}
+
+// similarity of two words: every masked field within its threshold
+// (graph_functions.cu:291-293)
+__device__ __forceinline__ bool similar(uint32_t a, uint32_t b, uint32_t thr)
+{
+    return (__vcmpleu4(__vabsdiffu4(a, b), thr) & 0x00FFFFFFu) == 0x00FFFFFFu;
+}
+
+// Reference-layout bytes of one pixel (b0, b1, b2) packed little-endian.
+__device__ __forceinline__ uint32_t load_bgr(const uint8_t* img, int ws, int layout, int i, int j)
+{
+    if (layout == DEPIX_LAYOUT_RGBA) {
+        uint32_t p = __ldg(reinterpret_cast<const uint32_t*>(img + (size_t)j * ws) + i);
+        // RGBA -> B,G,R
+        return ((p >> 16) & 0xFFu) | (p & 0xFF00u) | ((p & 0xFFu) << 16);
+    }
+    const uint8_t* q = img + (size_t)j * ws + 3 * i;
+    return (uint32_t)__ldg(q) | ((uint32_t)__ldg(q + 1) << 8) | ((uint32_t)__ldg(q + 2) << 16);
+}
+
+__device__ __forceinline__ uint32_t word_of_bgr(uint32_t c)
+{
+    return yuv_word((int)(c & 0xFF), (int)((c >> 8) & 0xFF), (int)((c >> 16) & 0xFF));
+}
+
+// Byte at linear offset `off` of the reference's BGR image (rows `vws` bytes,
+// 3*w used, zero padding), zero outside the image. For RGBA input the
+// reference image is the 4-byte-aligned BGR image it would have loaded.
+__device__ __forceinline__ int ref_byte(const uint8_t* img, int w, int h, int ws, int layout, long long off)
+{
+    if (layout == DEPIX_LAYOUT_BGR) {
+        if (off < 0 || off >= (long long)h * ws) return 0;
+        return __ldg(img + off);
+    }
+    int vws = (3 * w + 3) & ~3;
+    if (off < 0 || off >= (long long)h * vws) return 0;
+    int row = (int)(off / vws), col = (int)(off % vws);
+    if (col >= 3 * w) return 0;
+    int px = col / 3, ch = col % 3; // ch 0 = B, 1 = G, 2 = R
+    return __ldg(img + (size_t)row * ws + 4 * px + (2 - ch));
+}
+
+__device__ __forceinline__ int ref_stride(int w, int ws, int layout)
+{
+    return layout == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
+}
+
+// 3-byte colour equality at two linear offsets (isColorEqual, subdivision_functions.cu:157-167)
+__device__ __forceinline__ bool ref_color_eq(const uint8_t* img, int w, int h, int ws, int layout, long long a,
+                                             long long b)
+{
+    return ref_byte(img, w, h, ws, layout, a) == ref_byte(img, w, h, ws, layout, b) &&
+           ref_byte(img, w, h, ws, layout, a + 1) == ref_byte(img, w, h, ws, layout, b + 1) &&
+           ref_byte(img, w, h, ws, layout, a + 2) == ref_byte(img, w, h, ws, layout, b + 2);
+}
+
+// T-junction test at vertex (cx, cy) of cell (i, j) (checkTJunction,
+// subdivision_functions.cu:170-242): its bounds test (written with the width
+// in place of the stride) answers true for any vertex; past it only the four
+// corners can answer true. Reads the image through linear offsets.
+static __device__ __noinline__ bool t_junction_global(const uint8_t* img, int w, int h, int ws, int layout, int i, int j,
+                                               int cx, int cy)
+{
+    long long st = ref_stride(w, ws, layout);
+    long long index = (long long)j * st + (long long)i * 3;
+    if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
+    long long c0 = index + st - 3, c1 = index + st, c2 = index + st + 3, c3 = index - 3, c4 = index + 3;
+    long long c5 = index - st - 3, c6 = index - st, c7 = index - st + 3;
+#define EQ(a, b) ref_color_eq(img, w, h, ws, layout, a, b)
+    if (cx == 0 && cy == 0 && (!EQ(c3, c5) || !EQ(c5, c6))) return true;
+    if (cx == kUnit && cy == 0 && (!EQ(c4, c7) || !EQ(c7, c6))) return true;
+    if (cx == kUnit && cy == kUnit && (!EQ(c1, c2) || !EQ(c2, c4))) return true;
+    if (cx == 0 && cy == kUnit && (!EQ(c0, c1) || !EQ(c1, c3))) return true;
+#undef EQ
+    return false;
+}
+
+// ------------------------------------------------------- cell pattern tables
+
+// Pattern of a cell: node byte (bits 0-7), left neighbour bit 2 (8) and
+// bit 7 (9), right neighbour bit 0 (10) and bit 5 (11): all that decides its
+// reshaped polygon (createCellFromPattern, diagram_functions.cu:320-520).
+__device__ __forceinline__ int cell_pattern(unsigned node, unsigned left, unsigned right)
+{
+    return (int)(node & 0xFF) | (bitof(left, 2) << 8) | (bitof(left, 7) << 9) | (bitof(right, 0) << 10) |
+           (bitof(right, 5) << 11);
+}
+
+// A cell polygon in 1/64-cell units.
+struct Poly {
+    int n;
+    int x[kMaxPoly];
+    int y[kMaxPoly];
+};
+
+// Decodes a hull table entry (built once per device in depix_geom.cu):
+// vertex count in bits 0-3, then 8 vertices of 6 bits (x+1 | (y+1) << 3,
+// quarter units).
+__device__ __forceinline__ void hull_from_lut(uint64_t e, Poly& p)
+{
+    p.n = (int)(e & 0xF);
+#pragma unroll
+    for (int t = 0; t < kMaxHull; t++) {
+        unsigned v = (unsigned)(e >> (4 + 6 * t)) & 63u;
+        p.x[t] = ((int)(v & 7) - 1) * (kUnit / 4);
+        p.y[t] = ((int)(v >> 3) - 1) * (kUnit / 4);
+    }
+}
+
+// ------------------------------------------------------------- subdivision
+
+__device__ __forceinline__ int pmod(int i, int n) { return (n + (i % n)) % n; }
+
+// Neighbour direction an edge is shared with, or -1 (isLinkedEdge,
+// subdivision_functions.cu:245-424). In integer units the float slope test
+// "== +-1" is dy == +-dx with dx != 0, and the 0.5 tests compare with 32.
+__device__ __forceinline__ int edge_link(const Poly& c, unsigned node, int idx)
+{
+    int b = pmod(idx + 1, c.n);
+    int ax = c.x[idx], ay = c.y[idx], bx = c.x[b], by = c.y[b];
+    int dx = bx - ax, dy = by - ay, my2 = ay + by;
+    const int half = kUnit / 2;
+    if (ay == by && ay > half && bitof(node, 1)) return 1;
+    if (ax == bx && ax > half && bitof(node, 4)) return 4;
+    if (ay == by && ay < half && bitof(node, 6)) return 6;
+    if (ax == bx && ax < half && bitof(node, 3)) return 3;
+    bool s1 = dx != 0 && dy == dx, sm1 = dx != 0 && dy == -dx;
+    if (s1 && my2 > kUnit && bitof(node, 0)) return 0;
+    if (sm1 && my2 > kUnit && bitof(node, 2)) return 2;
+    if (s1 && my2 < kUnit && bitof(node, 7)) return 7;
+    if (sm1 && my2 < kUnit && bitof(node, 5)) return 5;
+    return -1;
+}
+
+// corner-cutting points on edge i -> i+1 (getQ_i / getR_i,
+// subdivision_functions.cu:42-122): 3/4-1/4 when the edge is at most one cell
+// long, else 7/8-1/8.
+__device__ __forceinline__ void qr_point(const Poly& c, int i, bool want_r, int& ox, int& oy)
+{
+    int a = i % c.n;
+    if (a < 0) a += c.n;
+    int b = (i + 1) % c.n;
+    int px = c.x[a], py = c.y[a], nx = c.x[b], ny = c.y[b];
+    int l2 = (nx - px) * (nx - px) + (ny - py) * (ny - py);
+    if (l2 <= kUnit * kUnit) {
+        if (want_r) { ox = (px + 3 * nx) / 4; oy = (py + 3 * ny) / 4; }
+        else { ox = (3 * px + nx) / 4; oy = (3 * py + ny) / 4; }
+    } else {
+        if (want_r) { ox = (px + 7 * nx) / 8; oy = (py + 7 * ny) / 8; }
+        else { ox = (7 * px + nx) / 8; oy = (7 * py + ny) / 8; }
+    }
+}
+
+// Q (or R) point of a linked neighbour's hull around the vertex matching
+// (px, py), mapped back to this cell (get{Q,R}_i_from_linked_cell,
+// subdivision_functions.cu:125-154; getPointIndex falls back to index 0).
+__device__ __forceinline__ void linked_point(const Poly& nb, int link, int px, int py, bool want_r, int& ox,
+                                             int& oy)
+{
+    int tx = px - kUnit * dir_di(link), ty = py - kUnit * dir_dj(link);
+    int op = 0;
+    for (int t = 0; t < nb.n; t++)
+        if (nb.x[t] == tx && nb.y[t] == ty) { op = t; break; }
+    qr_point(nb, want_r ? op - 1 : op, want_r, ox, oy);
+    ox += kUnit * dir_di(link);
+    oy += kUnit * dir_dj(link);
+}
+
+// One corner-cutting round of a cell (subdivision, subdivision_functions.cu:564-669).
+// NbHull(link, Poly&) fetches the hull of the neighbour in direction link;
+// TJ(cx, cy) is the T-junction test at a cell corner.
+template <typename NbHull, typename TJ>
+__device__ void subdivide_cell(const Poly& c, unsigned node, NbHull nb_hull, TJ tj, Poly& out)
+{
+    int link[kMaxHull];
+    for (int e = 0; e < c.n; e++) link[e] = edge_link(c, node, e);
+    int m = 0;
+    Poly nb;
+    for (int v = 0; v < c.n; v++) {
+        int lp = link[pmod(v - 1, c.n)];
+        bool cur = link[v] >= 0, prev = lp >= 0;
+        int px = c.x[v], py = c.y[v];
+        if (!cur && !prev) {
+            // the test's image-bounds check answers "keep" for any vertex of
+            // the cells it covers, before it looks at corners
+            if (tj(px, py)) {
+                out.x[m] = px; out.y[m] = py; m++;
+            } else {
+                int rx, ry, qx, qy;
+                qr_point(c, v - 1, true, rx, ry);
+                qr_point(c, v, false, qx, qy);
+                out.x[m] = rx; out.y[m] = ry; m++;
+                out.x[m] = qx; out.y[m] = qy; m++;
+            }
+        } else if (!cur && prev) {
+            int qx, qy, ax, ay;
+            qr_point(c, v, false, qx, qy);
+            nb_hull(lp, nb);
+            linked_point(nb, lp, px, py, true, ax, ay);
+            out.x[m] = (qx + ax) / 2; out.y[m] = (qy + ay) / 2; m++;
+            out.x[m] = qx; out.y[m] = qy; m++;
+        } else if (cur && !prev) {
+            int rx, ry, ax, ay;
+            nb_hull(link[v], nb);
+            linked_point(nb, link[v], px, py, false, ax, ay);
+            qr_point(c, v - 1, true, rx, ry);
+            out.x[m] = rx; out.y[m] = ry; m++;
+            out.x[m] = (rx + ax) / 2; out.y[m] = (ry + ay) / 2; m++;
+        } else {
+            out.x[m] = px; out.y[m] = py; m++;
+        }
+    }
+    out.n = m;
+}
+
+// ----------------------------------------------------------- ear clipping
+
+__device__ __forceinline__ bool inside_tri(int Ax, int Ay, int Bx, int By, int Cx, int Cy, int Px, int Py)
+{
+    int a = (Cx - Bx) * (Py - By) - (Cy - By) * (Px - Bx);
+    int c = (Bx - Ax) * (Py - Ay) - (By - Ay) * (Px - Ax);
+    int b = (Ax - Cx) * (Py - Cy) - (Ay - Cy) * (Px - Cx);
+    return a >= 0 && b >= 0 && c >= 0;
+}
+
+// Ear clipping (process / snip / area, triangulate_functions.cu:6-217) in
+// integer units: the reference's EPSILON test on an exact product of
+// 1/64-multiples is "cross <= 0". Writes corner indices, returns the triangle
+// count; ok = false when the reference's loop guard gives up.
+__device__ __forceinline__ int ear_clip(const Poly& c, uint8_t* tri, bool& ok)
+{
+    ok = true;
+    int n = c.n;
+    if (n < 3) { ok = false; return 0; }
+    int area = 0;
+    for (int p = n - 1, q = 0; q < n; p = q++) area += c.x[p] * c.y[q] - c.x[q] * c.y[p];
+    int V[kMaxPoly];
+    for (int v = 0; v < n; v++) V[v] = area > 0 ? v : (n - 1) - v;
+    int nv = n, nt = 0, count = 2 * nv;
+    for (int v = nv - 1; nv > 2;) {
+        if (0 >= (count--)) { ok = false; return nt; }
+        int u = v;
+        if (nv <= u) u = 0;
+        v = u + 1;
+        if (nv <= v) v = 0;
+        int w = v + 1;
+        if (nv <= w) w = 0;
+        int Ax = c.x[V[u]], Ay = c.y[V[u]], Bx = c.x[V[v]], By = c.y[V[v]], Cx = c.x[V[w]], Cy = c.y[V[w]];
+        bool ear = ((Bx - Ax) * (Cy - Ay) - (By - Ay) * (Cx - Ax)) > 0;
+        if (ear)
+            for (int p = 0; p < nv; p++) {
+                if (p == u || p == v || p == w) continue;
+                if (inside_tri(Ax, Ay, Bx, By, Cx, Cy, c.x[V[p]], c.y[V[p]])) { ear = false; break; }
+            }
+        if (ear) {
+            tri[3 * nt] = (uint8_t)V[u];
+            tri[3 * nt + 1] = (uint8_t)V[v];
+            tri[3 * nt + 2] = (uint8_t)V[w];
+            nt++;
+            for (int s = v, t = v + 1; t < nv; s++, t++) V[s] = V[t];
+            nv--;
+            count = 2 * nv;
+        }
+    }
+    return nt;
+}
+
+// ------------------------------------------------------------------ raster
+
+// Sample coverage of one triangle under the top-left rule, all in integer
+// units of 1/256 output pixel relative to a common origin. The triangle is
+// taken counter-clockwise (y up); zero area covers nothing.
+__device__ __forceinline__ bool covers(int ax, int ay, int bx, int by, int cx, int cy, int sx, int sy)
+{
+    int area = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+    if (area == 0) return false;
+    if (area < 0) {
+        int tx = bx, ty = by;
+        bx = cx; by = cy; cx = tx; cy = ty;
+    }
+    int ex, ey, f;
+    ex = bx - ax; ey = by - ay; f = ex * (sy - ay) - ey * (sx - ax);
+    if (!(f > 0 || (f == 0 && (ey < 0 || (ey == 0 && ex < 0))))) return false;
+    ex = cx - bx; ey = cy - by; f = ex * (sy - by) - ey * (sx - bx);
+    if (!(f > 0 || (f == 0 && (ey < 0 || (ey == 0 && ex < 0))))) return false;
+    ex = ax - cx; ey = ay - cy; f = ex * (sy - cy) - ey * (sx - cx);
+    if (!(f > 0 || (f == 0 && (ey < 0 || (ey == 0 && ex < 0))))) return false;
+    return true;
+}
+
+}  // namespace depix

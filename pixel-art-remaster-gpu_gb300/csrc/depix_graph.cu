@@ -1,0 +1,351 @@
+// depix_graph.cu -- similarity graph, crossing resolution and component
+// labelling kernels.
+//
+// Frames are addressed through FrameRef so the same tile functions serve a
+// single frame (grid.z = 1) and a batch of equal-size frames (grid.z = frame).
+#include "depix_internal.h"
+
+namespace depix {
+
+// ------------------------------------------------------------ graph stage
+
+// Pair bits of one pixel p inside the tile region: similarity with the
+// right (bit 0), upper (bit 1), upper-right (bit 2) pixel, and of the pair
+// (right, upper) (bit 3), each only when both pixels are in the image.
+constexpr int kGTW = 64;  // graph tile width (pixels)
+constexpr int kGTH = 8;   // graph tile height
+
+template <int LAYOUT>
+__device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uint32_t thr, bool fuse_trivial)
+{
+    constexpr int RW = kGTW + 2, RH = kGTH + 2;
+    __shared__ uint32_t words[RH][RW];
+    __shared__ uint8_t pairs[RH][RW];
+    const int w = f.w, h = f.h;
+    for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
+        int rx = k % RW, ry = k / RW;
+        int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+        uint32_t wd = 0;
+        if (gx >= 0 && gy >= 0 && gx < w && gy < h) wd = word_of_bgr(load_bgr(f.img, f.ws, LAYOUT, gx, gy));
+        words[ry][rx] = wd;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
+        int rx = k % RW, ry = k / RW;
+        int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+        unsigned pb = 0;
+        bool in = gx >= 0 && gy >= 0 && gx < w && gy < h;
+        bool rin = rx + 1 < RW && gx + 1 < w && gx + 1 >= 0 && in;
+        bool uin = ry + 1 < RH && gy + 1 < h && gy + 1 >= 0 && in;
+        if (rin && similar(words[ry][rx], words[ry][rx + 1], thr)) pb |= 1u;
+        if (uin && similar(words[ry][rx], words[ry + 1][rx], thr)) pb |= 2u;
+        if (rin && uin) {
+            if (similar(words[ry][rx], words[ry + 1][rx + 1], thr)) pb |= 4u;
+            if (similar(words[ry][rx + 1], words[ry + 1][rx], thr)) pb |= 8u;
+        }
+        pairs[ry][rx] = (uint8_t)pb;
+    }
+    __syncthreads();
+    // node bits (graph_Kernel) and, fused, the trivial removal (crossCheck_4):
+    // a diagonal goes when the 2x2 block it crosses has all four sides similar
+    for (int k = threadIdx.x; k < kGTW * kGTH; k += blockDim.x) {
+        int tx = k % kGTW, ty = k / kGTW;
+        int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= w || gy >= h) continue;
+        int rx = tx + 1, ry = ty + 1;
+        unsigned c = pairs[ry][rx], l = pairs[ry][rx - 1], d = pairs[ry - 1][rx], dl = pairs[ry - 1][rx - 1];
+        unsigned node = 0;
+        node |= (unsigned)bitof(c, 1) << 1;   // up
+        node |= (unsigned)bitof(d, 1) << 6;   // down
+        node |= (unsigned)bitof(c, 0) << 4;   // right
+        node |= (unsigned)bitof(l, 0) << 3;   // left
+        node |= (unsigned)bitof(c, 2) << 2;   // up-right
+        node |= (unsigned)bitof(l, 3) << 0;   // up-left: pair (right of l = c, up of l)
+        node |= (unsigned)bitof(dl, 2) << 5;  // down-left
+        node |= (unsigned)bitof(d, 3) << 7;   // down-right: pair (right of d, up of d = c)
+        if (fuse_trivial) {
+            // block with lower-left (bx, by) full: H(bx,by) H(bx,by+1) V(bx,by) V(bx+1,by)
+            auto full = [&](int bx, int by) {
+                return bitof(pairs[by][bx], 0) && bitof(pairs[by + 1][bx], 0) && bitof(pairs[by][bx], 1) &&
+                       bitof(pairs[by][bx + 1], 1);
+            };
+            if (full(rx, ry)) node &= ~4u;
+            if (full(rx - 1, ry)) node &= ~1u;
+            if (full(rx - 1, ry - 1)) node &= ~32u;
+            if (full(rx, ry - 1)) node &= ~128u;
+        }
+        f.graph[(size_t)gy * w + gx] = (uint8_t)node;
+    }
+}
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) k_graph(FrameBatch b, uint32_t thr, int fuse_trivial)
+{
+    FrameRef f = b.frame(blockIdx.z);
+    graph_tile<LAYOUT>(f, blockIdx.x * kGTW, blockIdx.y * kGTH, thr, fuse_trivial != 0);
+}
+
+// Trivial removal on a graph in place (crossCheck_4, graph_functions.cu:1211-1274).
+// Only orthogonal bits are read and only diagonal bits written: race-free.
+__global__ void k_trivial(uint8_t* g, int w, int h)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= w || j >= h) return;
+    auto at = [&](int x, int y) -> unsigned {
+        return (x < 0 || y < 0 || x >= w || y >= h) ? 0u : (unsigned)g[(size_t)y * w + x];
+    };
+    unsigned c = at(i, j), l = at(i - 1, j), r = at(i + 1, j), u = at(i, j + 1), d = at(i, j - 1);
+    unsigned ul = at(i - 1, j + 1), ur = at(i + 1, j + 1), dl = at(i - 1, j - 1), dr = at(i + 1, j - 1);
+    unsigned out = c;
+    if (bitof(l, 1) && bitof(l, 4) && bitof(ul, 6) && bitof(ul, 4) && bitof(c, 3) && bitof(c, 1) && bitof(u, 6) &&
+        bitof(u, 3))
+        out &= ~1u;
+    if (bitof(c, 1) && bitof(c, 4) && bitof(u, 6) && bitof(u, 4) && bitof(r, 3) && bitof(r, 1) && bitof(ur, 6) &&
+        bitof(ur, 3))
+        out &= ~4u;
+    if (bitof(dl, 1) && bitof(dl, 4) && bitof(l, 6) && bitof(l, 4) && bitof(d, 3) && bitof(d, 1) && bitof(c, 6) &&
+        bitof(c, 3))
+        out &= ~32u;
+    if (bitof(d, 1) && bitof(d, 4) && bitof(c, 6) && bitof(c, 4) && bitof(dr, 3) && bitof(dr, 1) && bitof(r, 6) &&
+        bitof(r, 3))
+        out &= ~128u;
+    if (out != c) g[(size_t)j * w + i] = (uint8_t)out;
+}
+
+// ------------------------------------------------------- heuristics stage
+
+constexpr int kHTW = 64, kHTH = 16;
+constexpr int kHalo = 32; // a curve-length walk moves at most 31 steps from a block node
+constexpr int kHRW = kHTW + 2 * kHalo, kHRH = kHTH + 2 * kHalo;
+
+struct SnapTile {
+    const uint8_t (*s)[kHRW];
+    int ox, oy; // image coordinates of s[0][0]
+    __device__ __forceinline__ unsigned at(int x, int y) const { return s[y - oy][x - ox]; }
+};
+
+// set bits of node other than bit e; last = the highest such bit in the
+// scan order e+1 .. e+7 (mod 8)
+__device__ __forceinline__ int others(unsigned node, int e, int& last)
+{
+    unsigned rest = (node & 0xFFu) & ~(1u << e);
+    int s = __popc(rest);
+    if (s) {
+        // scan order e+1, ..., 7, 0, ..., e-1: the last in that order is the
+        // highest set bit below e if any, else the highest set bit overall
+        unsigned below = rest & ((1u << e) - 1u);
+        last = below ? 31 - __clz(below) : 31 - __clz(rest);
+    }
+    return s;
+}
+
+// curve-length walk (calcVal2PathSize, graph_functions.cu:541-573)
+__device__ __forceinline__ void walk_len(const SnapTile& t, int i, int j, int e, int& result)
+{
+    for (;;) {
+        int k_n = 0;
+        int s = others(t.at(i, j), e, k_n);
+        if (result > 30) return;
+        if (s != 1) return;
+        result++;
+        i += dir_di(k_n);
+        j += dir_dj(k_n);
+        e = 7 - k_n;
+    }
+}
+
+// block decision (processHeuristics2, graph_functions.cu:761-849): true
+// removes "/" (bits 2/5), false removes "\" (bits 0/7)
+__device__ bool block_decision(const SnapTile& t, int i, int j)
+{
+    unsigned n1 = t.at(i, j), n2 = t.at(i, j + 1), n3 = t.at(i + 1, j), n4 = t.at(i + 1, j + 1);
+    int dummy;
+    int o1 = others(n1, 2, dummy), o4 = others(n4, 5, dummy), o3 = others(n3, 0, dummy), o2 = others(n2, 7, dummy);
+    if (o1 == 1 && o4 == 1) return false;      // curve through "/"
+    if (o3 == 1 && o2 == 1) return true;       // curve through "\"
+    bool v1 = o1 == 0, v4 = o4 == 0, v3 = o3 == 0, v2 = o2 == 0;
+    if ((v1 || v4) && !v3 && !v2) return false; // island
+    if (v3 || (v2 && !v1 && !v4)) return true;  // island, reference precedence (graph_functions.cu:805)
+    int seg = 0, seg2 = 0;
+    walk_len(t, i, j, 2, seg);
+    walk_len(t, i + 1, j + 1, 5, seg);
+    walk_len(t, i + 1, j, 0, seg2);
+    walk_len(t, i, j + 1, 7, seg2);
+    return !(seg2 < seg);
+}
+
+__device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* out, int w, int h, int x0, int y0)
+{
+    __shared__ __align__(16) uint8_t s[kHRH][kHRW];
+    const int ox = x0 - kHalo, oy = y0 - kHalo;
+    // 4-byte loads where a row is word aligned in memory, else bytes
+    for (int k = threadIdx.x; k < kHRH * (kHRW / 4); k += blockDim.x) {
+        int ry = k / (kHRW / 4), rx = 4 * (k % (kHRW / 4));
+        int gy = oy + ry, gx = ox + rx;
+        uint32_t v = 0;
+        if (gy >= 0 && gy < h) {
+            const uint8_t* row = snap + (size_t)gy * w;
+            if (gx >= 0 && gx + 3 < w && ((reinterpret_cast<uintptr_t>(row + gx) & 3) == 0)) {
+                v = __ldg(reinterpret_cast<const uint32_t*>(row + gx));
+            } else {
+                for (int q = 0; q < 4; q++)
+                    if (gx + q >= 0 && gx + q < w) v |= (uint32_t)__ldg(row + gx + q) << (8 * q);
+            }
+        }
+        *reinterpret_cast<uint32_t*>(&s[ry][rx]) = v;
+    }
+    __syncthreads();
+    SnapTile t{s, ox, oy};
+    for (int k = threadIdx.x; k < kHTW * kHTH; k += blockDim.x) {
+        int i = x0 + k % kHTW, j = y0 + k / kHTW;
+        if (i >= w || j >= h) continue;
+        unsigned c = t.at(i, j), o = c;
+        // only nodes with a diagonal can be touched
+        if (c & 0xA5u) {
+            if (bitof(t.at(i - 1, j), 2) && bitof(t.at(i - 1, j + 1), 7) && bitof(c, 0) && bitof(t.at(i, j + 1), 5))
+                if (!block_decision(t, i - 1, j)) o &= ~1u;
+            if (bitof(t.at(i - 1, j - 1), 2) && bitof(t.at(i - 1, j), 7) && bitof(t.at(i, j - 1), 0) && bitof(c, 5))
+                if (block_decision(t, i - 1, j - 1)) o &= ~32u;
+            if (bitof(t.at(i, j - 1), 2) && bitof(c, 7) && bitof(t.at(i + 1, j - 1), 0) && bitof(t.at(i + 1, j), 5))
+                if (!block_decision(t, i, j - 1)) o &= ~128u;
+            if (bitof(c, 2) && bitof(t.at(i, j + 1), 7) && bitof(t.at(i + 1, j), 0) && bitof(t.at(i + 1, j + 1), 5))
+                if (block_decision(t, i, j)) o &= ~4u;
+        }
+        out[(size_t)j * w + i] = (uint8_t)o;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_heuristics(GraphBatch b)
+{
+    const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
+    uint8_t* out = b.out + b.frame_stride * blockIdx.z;
+    heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH);
+}
+
+// -------------------------------------------------- component labelling
+
+__device__ __forceinline__ int uf_find(int32_t* L, int x)
+{
+    int p = L[x];
+    while (p != x) {
+        x = p;
+        p = L[x];
+    }
+    return x;
+}
+
+// lock-free union with the smaller root winning: the final root of every
+// component is its minimum index
+__device__ __forceinline__ void uf_unite(int32_t* L, int a, int b)
+{
+    for (;;) {
+        a = uf_find(L, a);
+        b = uf_find(L, b);
+        if (a == b) return;
+        if (a > b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        int old = atomicMin(&L[b], a);
+        if (old == b) return;
+        b = old;
+    }
+}
+
+__global__ void k_cc_init(int32_t* L, int n, size_t frame_stride)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) L[frame_stride * blockIdx.z + k] = k;
+}
+
+// each node unites with its right, up-right, up and up-left neighbours
+__global__ void k_cc_unite(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w * h) return;
+    g += frame_stride * blockIdx.z;
+    L += frame_stride * blockIdx.z;
+    int i = k % w, j = k / w;
+    unsigned node = g[k];
+    const int dirs[4] = {4, 2, 1, 0};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        int e = dirs[q];
+        if (!bitof(node, e)) continue;
+        int ni = i + dir_di(e), nj = j + dir_dj(e);
+        if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
+        uf_unite(L, k, nj * w + ni);
+    }
+    // a bit set toward a lower neighbour without its mirror still joins the two
+#pragma unroll
+    for (int e = 3; e <= 7; e++) {
+        if (e == 4) continue;
+        if (!bitof(node, e)) continue;
+        int ni = i + dir_di(e), nj = j + dir_dj(e);
+        if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
+        if (bitof(g[nj * w + ni], 7 - e)) continue; // the neighbour's forward edge covers it
+        uf_unite(L, k, nj * w + ni);
+    }
+}
+
+__global__ void k_cc_flatten(int32_t* L, int n, size_t frame_stride)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    L += frame_stride * blockIdx.z;
+    L[k] = uf_find(L, k);
+}
+
+__global__ void k_yuv_words(const uint8_t* px3, size_t n, uint32_t* out)
+{
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    out[k] = yuv_word(px3[3 * k], px3[3 * k + 1], px3[3 * k + 2]);
+}
+
+// ----------------------------------------------------------------- launch
+
+cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, uint32_t* out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_yuv_words<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(px3, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_graph(const FrameBatch& b, int nframes, uint32_t thr, bool fuse_trivial, cudaStream_t s)
+{
+    dim3 grid((b.w + kGTW - 1) / kGTW, (b.h + kGTH - 1) / kGTH, nframes);
+    if (b.layout == DEPIX_LAYOUT_RGBA)
+        k_graph<DEPIX_LAYOUT_RGBA><<<grid, 256, 0, s>>>(b, thr, fuse_trivial ? 1 : 0);
+    else
+        k_graph<DEPIX_LAYOUT_BGR><<<grid, 256, 0, s>>>(b, thr, fuse_trivial ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trivial(uint8_t* g, int w, int h, cudaStream_t s)
+{
+    dim3 blk(32, 8), grid((w + 31) / 32, (h + 7) / 8);
+    k_trivial<<<grid, blk, 0, s>>>(g, w, h);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s)
+{
+    dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
+    k_heuristics<<<grid, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int nframes, size_t frame_stride,
+                          cudaStream_t s)
+{
+    int n = w * h;
+    dim3 grid((n + 255) / 256, 1, nframes);
+    k_cc_init<<<grid, 256, 0, s>>>(labels, n, frame_stride);
+    k_cc_unite<<<grid, 256, 0, s>>>(g, labels, w, h, frame_stride);
+    k_cc_flatten<<<grid, 256, 0, s>>>(labels, n, frame_stride);
+    return cudaGetLastError();
+}
+
+}  // namespace depix

@@ -1,0 +1,231 @@
+"""Python binding of libdepix.so (the C ABI declared in include/depix.h).
+
+Device buffers are passed as torch CUDA tensors (or raw integer addresses);
+streams as torch.cuda.Stream (default: torch's current stream). There is no
+CPU fallback: when the library is missing every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "libdepix.so")
+
+LAYOUT_BGR = 0
+LAYOUT_RGBA = 1
+CELL = 45
+
+
+class DepixError(RuntimeError):
+    def __init__(self, status, where, detail=""):
+        self.status = status
+        super().__init__(f"{where}: status {status} ({_status_name(status)}) {detail}".strip())
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("tr_y", ctypes.c_int), ("tr_u", ctypes.c_int), ("tr_v", ctypes.c_int),
+                ("subdivide", ctypes.c_int), ("scale", ctypes.c_int)]
+
+
+def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4) -> Params:
+    return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale)
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+
+
+def _sig(L, name, args, res=ctypes.c_int):
+    fn = getattr(L, name)
+    fn.argtypes = args
+    fn.restype = res
+
+
+def lib():
+    """Load libdepix.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} not built: run pixel-art-remaster-gpu_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER(Params)
+        _sig(L, "depix_default_params", [P], None)
+        _sig(L, "depix_status_string", [_i], ctypes.c_char_p)
+        _sig(L, "depix_last_error", [], ctypes.c_char_p)
+        _sig(L, "depix_init_device", [])
+        _sig(L, "depix_graph", [_vp, _i, _i, _i, _i, P, _i, _vp, _vp])
+        _sig(L, "depix_resolve_trivial", [_vp, _i, _i, _vp])
+        _sig(L, "depix_resolve_heuristics", [_vp, _i, _i, _vp, _vp])
+        _sig(L, "depix_cells", [_vp, _i, _i, _vp, _vp, _vp])
+        _sig(L, "depix_subdivide", [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_triangulate", [_vp, _vp, _i, _i, _vp])
+        _sig(L, "depix_emit_vbo", [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_label_components", [_vp, _i, _i, _vp, _vp])
+        _sig(L, "depix_raster", [_vp, _i, _i, _i, _i, _vp, P, _vp, _vp])
+        _sig(L, "depix_context_create", [ctypes.POINTER(_vp), ctypes.c_size_t, _i])
+        _sig(L, "depix_context_destroy", [_vp])
+        _sig(L, "depix_frame", [_vp, _vp, _i, _i, _i, _i, P, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_batch", [_vp, _i, _vp, _vp, _vp, _vp, _vp, P, _vp, _vp, _vp])
+        _sig(L, "depix_batch_host", [_vp, _i, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, P, _vp, ctypes.c_size_t,
+                                     _vp, _vp])
+        _sig(L, "depix_context_set_timing", [_vp, _i])
+        _sig(L, "depix_context_stage_times", [_vp, _vp, _vp, _vp])
+        _sig(L, "depix_launch_kernel_compat", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, _i, P], _vp)
+        _sig(L, "launch_kernel", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, ctypes.c_bool], _vp)
+        _sig(L, "depix_yuv_words", [_vp, ctypes.c_size_t, _vp, _vp])
+        _sig(L, "depix_pattern_tables", [_vp, _vp])
+        _lib = L
+    return _lib
+
+
+def _status_name(s):
+    try:
+        return lib().depix_status_string(s).decode()
+    except Exception:
+        return "?"
+
+
+def _check(status, where):
+    if status != 0:
+        raise DepixError(status, where, lib().depix_last_error().decode())
+
+
+def ptr(t):
+    """Device/host address of a torch tensor, numpy array or int."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return _vp(t)
+    if hasattr(t, "data_ptr"):
+        return _vp(t.data_ptr())
+    if hasattr(t, "ctypes"):
+        return _vp(t.ctypes.data)
+    raise TypeError(type(t))
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return _vp(s.cuda_stream)
+
+
+def init_device():
+    _check(lib().depix_init_device(), "depix_init_device")
+
+
+def graph(img, w, h, ws, layout, p, out, fuse_trivial=True, stream=None):
+    _check(lib().depix_graph(ptr(img), w, h, ws, layout, ctypes.byref(p), int(fuse_trivial), ptr(out),
+                             stream_ptr(stream)), "depix_graph")
+
+
+def resolve_trivial(g, w, h, stream=None):
+    _check(lib().depix_resolve_trivial(ptr(g), w, h, stream_ptr(stream)), "depix_resolve_trivial")
+
+
+def resolve_heuristics(snap, w, h, out, stream=None):
+    _check(lib().depix_resolve_heuristics(ptr(snap), w, h, ptr(out), stream_ptr(stream)), "depix_resolve_heuristics")
+
+
+def cells(g, w, h, diagram, ec, stream=None):
+    _check(lib().depix_cells(ptr(g), w, h, ptr(diagram), ptr(ec), stream_ptr(stream)), "depix_cells")
+
+
+def subdivide(img, w, h, ws, layout, g, snap, ec_snap, diagram, ec, stream=None):
+    _check(lib().depix_subdivide(ptr(img), w, h, ws, layout, ptr(g), ptr(snap), ptr(ec_snap), ptr(diagram),
+                                 ptr(ec), stream_ptr(stream)), "depix_subdivide")
+
+
+def triangulate(diagram, ec, w, h, stream=None):
+    _check(lib().depix_triangulate(ptr(diagram), ptr(ec), w, h, stream_ptr(stream)), "depix_triangulate")
+
+
+def emit_vbo(img, w, h, ws, layout, diagram, ec, pos, col, stream=None):
+    _check(lib().depix_emit_vbo(ptr(img), w, h, ws, layout, ptr(diagram), ptr(ec), ptr(pos), ptr(col),
+                                stream_ptr(stream)), "depix_emit_vbo")
+
+
+def label_components(g, w, h, labels, stream=None):
+    _check(lib().depix_label_components(ptr(g), w, h, ptr(labels), stream_ptr(stream)), "depix_label_components")
+
+
+def raster(img, w, h, ws, layout, g, p, out, stream=None):
+    _check(lib().depix_raster(ptr(img), w, h, ws, layout, ptr(g), ctypes.byref(p), ptr(out), stream_ptr(stream)),
+           "depix_raster")
+
+
+def yuv_words(px, n, out, stream=None):
+    _check(lib().depix_yuv_words(ptr(px), n, ptr(out), stream_ptr(stream)), "depix_yuv_words")
+
+
+def pattern_tables(hull_out, tri_out):
+    _check(lib().depix_pattern_tables(ptr(hull_out), ptr(tri_out)), "depix_pattern_tables")
+
+
+class Context:
+    """Owns the scratch of the frame and batch paths."""
+
+    def __init__(self, max_pixels, max_frames=1):
+        h = _vp()
+        _check(lib().depix_context_create(ctypes.byref(h), max_pixels, max_frames), "depix_context_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().depix_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def frame(self, img, w, h, ws, layout, p, out, graph_out=None, labels=None, stream=None):
+        _check(lib().depix_frame(self.handle, ptr(img), w, h, ws, layout, ctypes.byref(p), ptr(out), ptr(graph_out),
+                                 ptr(labels), stream_ptr(stream)), "depix_frame")
+
+    @staticmethod
+    def _arrays(ws, hs, in_off, out_off):
+        n = len(ws)
+        return (n, (ctypes.c_int * n)(*ws), (ctypes.c_int * n)(*hs), (ctypes.c_uint64 * n)(*in_off),
+                (ctypes.c_uint64 * n)(*out_off))
+
+    def batch(self, ws, hs, in_off, out_off, img, p, out, labels=None, stream=None):
+        """ws/hs/in_off/out_off: host int sequences (frame sizes, byte offsets)."""
+        n, W, H, I, O = self._arrays(ws, hs, in_off, out_off)
+        _check(lib().depix_batch(self.handle, n, W, H, I, O, ptr(img), ctypes.byref(p), ptr(out), ptr(labels),
+                                 stream_ptr(stream)), "depix_batch")
+
+    def batch_host(self, ws, hs, in_off, out_off, h_img, in_bytes, p, h_out, out_bytes, h_labels=None,
+                   stream=None):
+        n, W, H, I, O = self._arrays(ws, hs, in_off, out_off)
+        _check(lib().depix_batch_host(self.handle, n, W, H, I, O, ptr(h_img), in_bytes, ctypes.byref(p),
+                                      ptr(h_out), out_bytes, ptr(h_labels), stream_ptr(stream)),
+               "depix_batch_host")
+
+    def set_timing(self, on=True):
+        _check(lib().depix_context_set_timing(self.handle, int(bool(on))), "depix_context_set_timing")
+
+    STAGES = ("graph", "heuristics", "labels", "raster")
+
+    def stage_times(self):
+        """{stage: (ms, launches, calls)} accumulated since the last call."""
+        ms = (ctypes.c_double * 4)()
+        la = (ctypes.c_longlong * 4)()
+        ca = (ctypes.c_longlong * 4)()
+        _check(lib().depix_context_stage_times(self.handle, ms, la, ca), "depix_context_stage_times")
+        return {name: (ms[k], la[k], ca[k]) for k, name in enumerate(self.STAGES)}
+
+
+def launch_kernel_compat(pos, col, img_host, w, h, ws, edge_count_host, graph_host, subdivide, p=None):
+    """Drop-in frame driver; returns the host address of the malloc'd points
+    (free it with libc free) or raises."""
+    r = lib().depix_launch_kernel_compat(ptr(pos), ptr(col), 0.0, ptr(img_host), w, h, ws, ptr(edge_count_host),
+                                         ptr(graph_host), int(bool(subdivide)),
+                                         ctypes.byref(p) if p is not None else None)
+    if not r:
+        raise DepixError(-1, "depix_launch_kernel_compat", lib().depix_last_error().decode())
+    return r

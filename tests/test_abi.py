@@ -1,0 +1,69 @@
+"""The C ABI without a GPU: the library loads, exports every function that
+include/depix.h declares, and rejects bad arguments before touching CUDA."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "depix.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b([A-Za-z_]\w*)\s*\(", src, flags=re.M)
+    return sorted({n for n in names if n not in ("defined",)})
+
+
+@pytest.fixture(scope="module")
+def L():
+    import build
+    build.build()
+    import depix
+    return depix.lib()
+
+
+def test_header_declares_the_drop_in_symbol():
+    names = declared_functions()
+    assert "launch_kernel" in names and "depix_raster" in names and len(names) >= 20
+
+
+def test_library_exports_every_declared_function(L):
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_status_strings(L):
+    assert L.depix_status_string(0) == b"ok"
+    assert L.depix_status_string(1) == b"invalid argument"
+
+
+def test_bad_arguments_are_rejected_before_cuda(L):
+    import depix
+    p = depix.params()
+    # NULL image
+    assert L.depix_graph(None, 4, 4, 16, 1, ctypes.byref(p), 1, ctypes.c_void_p(16), None) == 1
+    # zero size
+    assert L.depix_graph(ctypes.c_void_p(16), 0, 4, 16, 1, ctypes.byref(p), 1, ctypes.c_void_p(16), None) == 1
+    # RGBA stride too small
+    assert L.depix_graph(ctypes.c_void_p(16), 4, 4, 8, 1, ctypes.byref(p), 1, ctypes.c_void_p(16), None) == 1
+    # bad scale
+    bad = depix.params(scale=0)
+    assert L.depix_raster(ctypes.c_void_p(16), 4, 4, 16, 1, ctypes.c_void_p(16), ctypes.byref(bad),
+                          ctypes.c_void_p(16), None) == 1
+    # aliasing snapshot and output
+    assert L.depix_resolve_heuristics(ctypes.c_void_p(16), 4, 4, ctypes.c_void_p(16), None) == 1
+    # empty context
+    h = ctypes.c_void_p()
+    assert L.depix_context_create(ctypes.byref(h), 0, 1) == 1
+    assert b"capacity" in L.depix_last_error()
+
+
+def test_default_params(L):
+    import depix
+    p = depix.Params()
+    L.depix_default_params(ctypes.byref(p))
+    assert (p.tr_y, p.tr_u, p.tr_v, p.subdivide, p.scale) == (48, 7, 6, 1, 4)
