@@ -70,6 +70,50 @@ depix_status ensure_tables(cudaStream_t user)
     return DEPIX_OK;
 }
 
+// Per-device, per-scale coverage tables of the hull patterns, built once.
+std::mutex g_scale_mu;
+std::vector<std::vector<uint32_t*>> g_scale_lut; // [device][scale]
+
+depix_status scale_table(int scale, cudaStream_t user, const uint32_t** out)
+{
+    int dev = 0;
+    DEPIX_CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_scale_mu);
+    if (dev >= (int)g_scale_lut.size()) g_scale_lut.resize(dev + 1);
+    auto& v = g_scale_lut[dev];
+    if (v.size() <= (size_t)scale) v.resize(scale + 1, nullptr);
+    if (v[scale]) {
+        *out = v[scale];
+        return DEPIX_OK;
+    }
+    if (user) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        DEPIX_CK(cudaStreamIsCapturing(user, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+            t_last_error = "first raster at this scale inside a stream capture: run one frame at this scale first";
+            return DEPIX_ERR_CAPTURING;
+        }
+    }
+    uint32_t* lut = nullptr;
+    if (cudaMalloc(&lut, scale_mask_words(scale) * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        t_last_error = "cudaMalloc of the scale table failed";
+        return DEPIX_ERR_ALLOC;
+    }
+    cudaStream_t s;
+    DEPIX_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaError_t e = build_scale_masks(scale, lut, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        cudaFree(lut);
+        return cuda_fail(e, "build_scale_masks");
+    }
+    v[scale] = lut;
+    *out = lut;
+    return DEPIX_OK;
+}
+
 depix_status check_size(int w, int h)
 {
     if (w < 1 || h < 1) return arg_fail("width and height must be >= 1");
@@ -111,6 +155,20 @@ depix_status check_out_size(int w, int h, const depix_params* p)
 }
 
 inline cudaStream_t S(depix_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Coverage-mask raster up to scale 12, per-pixel gather beyond.
+depix_status raster_launch(const RasterBatch& b, int nframes, cudaStream_t s)
+{
+    DEPIX_TRY(ensure_tables(s));
+    if (b.scale <= kMaxMaskScale) {
+        const uint32_t* lut = nullptr;
+        DEPIX_TRY(scale_table(b.scale, s, &lut));
+        DEPIX_CK(launch_mask_raster(b, nframes, lut, s));
+    } else {
+        DEPIX_CK(launch_raster(b, nframes, s));
+    }
+    return DEPIX_OK;
+}
 
 }  // namespace
 
@@ -245,7 +303,7 @@ depix_status depix_raster(const uint8_t* d_img, int w, int h, int widthstep, dep
     DEPIX_TRY(check_out_size(w, h, p));
     DEPIX_TRY(ensure_tables(S(s)));
     RasterBatch b{d_img, 0, d_graph, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};
-    DEPIX_CK(launch_raster(b, 1, S(s)));
+    DEPIX_TRY(raster_launch(b, 1, S(s)));
     return DEPIX_OK;
 }
 
@@ -413,7 +471,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
             StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
             RasterBatch rb{img0, (size_t)is, ctx->graph_b, px, d_out + out_offset[0], (size_t)os, w[0], h[0],
                            4 * w[0], DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
-            DEPIX_CK(launch_raster(rb, n, s));
+            DEPIX_TRY(raster_launch(rb, n, s));
         }
         return DEPIX_OK;
     }
@@ -439,7 +497,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
             StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
             RasterBatch rb{img, 0, ctx->graph_b + goff, 0, d_out + out_offset[k], 0, w[k], h[k], 4 * w[k],
                            DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
-            DEPIX_CK(launch_raster(rb, 1, s));
+            DEPIX_TRY(raster_launch(rb, 1, s));
         }
         goff += ctx->max_pixels;
         loff += (size_t)w[k] * h[k];
@@ -554,7 +612,7 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
     if (d_out) {
         StageTimer t(ctx, DEPIX_STAGE_RASTER, 1, s);
         RasterBatch rb{d_img, 0, resolved, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};
-        DEPIX_CK(launch_raster(rb, 1, s));
+        DEPIX_TRY(raster_launch(rb, 1, s));
     }
     return DEPIX_OK;
 }

@@ -477,4 +477,368 @@ cudaError_t launch_raster(const RasterBatch& b, int nframes, cudaStream_t s)
     return cudaGetLastError();
 }
 
+
+// ------------------------------------------------------------ mask raster
+//
+// The gather above tests triangles per output pixel. This raster instead
+// reduces every cell to a coverage bitmask over the samples its polygon can
+// reach and resolves each output block with bit operations:
+//
+//  - a cell polygon lies inside [-0.75, 1.75]^2 of its own cell: hull points
+//    lie in [-0.25, 1.25], subdivision adds midpoints of an own point and a
+//    neighbour's point (neighbour hull shifted by one cell);
+//  - footprint: output samples (X+0.5)/s in that box, offsets m = X - i*s in
+//    [mlo, mlo + F); one 32-bit row word per footprint row (F <= 32, s <= 12);
+//  - plain cells (no subdivision) take their rows from a per-scale table over
+//    the 4096 hull patterns; subdivided cells are gathered into a list and
+//    cut, ear-clipped and masked one per thread;
+//  - an output block (the s x s samples of one cell) takes, per sample, the
+//    latest covering cell in VBO order among the 3x3 cells around it. A cell
+//    whose block its own mask fills and no neighbour polygon reaches is
+//    filled without per-sample work.
+
+struct MaskGeom {
+    int s;
+    int mlo, F;   // footprint of any cell polygon
+    int hlo, HF;  // footprint of a hull (no subdivision): [-0.25, 1.25]
+};
+
+__host__ __device__ __forceinline__ MaskGeom mask_geom(int s)
+{
+    MaskGeom g;
+    g.s = s;
+    g.mlo = -((3 * s + 2) / 4);
+    g.F = (7 * s - 2) / 4 - g.mlo + 1;
+    g.hlo = -((s + 2) / 4);
+    g.HF = (5 * s - 2) / 4 - g.hlo + 1;
+    return g;
+}
+
+// Sets the footprint samples (offsets mlo.. in both axes, F of them) that the
+// triangle covers under the top-left rule. Vertices in 1/256 output pixel
+// relative to the cell origin.
+__device__ __forceinline__ void tri_mask(int ax, int ay, int bx, int by, int cx, int cy, int mlo, int F,
+                                         uint32_t* rows)
+{
+    int area = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+    if (area == 0) return;
+    if (area < 0) {
+        int tx = bx, ty = by;
+        bx = cx; by = cy; cx = tx; cy = ty;
+    }
+    // E(p) = A px + B py + C; covered iff E >= bias on all three edges, where
+    // bias 0 on a top or left edge (dy < 0, or dy == 0 and dx < 0 with
+    // dx = B, dy = -A) and 1 elsewhere: E > 0, or E == 0 on a top/left edge
+    const int A0 = ay - by, B0 = bx - ax, C0 = -(A0 * ax + B0 * ay);
+    const int A1 = by - cy, B1 = cx - bx, C1 = -(A1 * bx + B1 * by);
+    const int A2 = cy - ay, B2 = ax - cx, C2 = -(A2 * cx + B2 * cy);
+    const int b0 = (A0 > 0 || (A0 == 0 && B0 < 0)) ? 0 : 1;
+    const int b1 = (A1 > 0 || (A1 == 0 && B1 < 0)) ? 0 : 1;
+    const int b2 = (A2 > 0 || (A2 == 0 && B2 < 0)) ? 0 : 1;
+    const int minx = min(ax, min(bx, cx)), maxx = max(ax, max(bx, cx));
+    const int miny = min(ay, min(by, cy)), maxy = max(ay, max(by, cy));
+    // sample offsets whose position 256 m + 128 lies inside the bounding box
+    // (>> on a signed int is a floor division by 256)
+    const int m0 = max(mlo, -((128 - minx) >> 8)), m1 = min(mlo + F - 1, (maxx - 128) >> 8);
+    const int n0 = max(mlo, -((128 - miny) >> 8)), n1 = min(mlo + F - 1, (maxy - 128) >> 8);
+    for (int n = n0; n <= n1; n++) {
+        int py = 256 * n + 128;
+        int e0 = B0 * py + C0, e1 = B1 * py + C1, e2 = B2 * py + C2;
+        uint32_t bits = 0;
+        for (int m = m0; m <= m1; m++) {
+            int px = 256 * m + 128;
+            if (A0 * px + e0 >= b0 && A1 * px + e1 >= b1 && A2 * px + e2 >= b2) bits |= 1u << (m - mlo);
+        }
+        rows[n - mlo] |= bits;
+    }
+}
+
+// Per-scale table: for each hull pattern, HF row words over the hull window.
+__global__ void k_build_scale_masks(int s, uint32_t* lut)
+{
+    int pat = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pat >= 4096) return;
+    MaskGeom g = mask_geom(s);
+    Poly c;
+    hull_from_lut(g_hull_lut[pat], c);
+    uint64_t te = g_tri_lut[pat];
+    uint32_t rows[32];
+    for (int r = 0; r < g.HF; r++) rows[r] = 0;
+    const int u = 4 * s;
+    for (int t = 0; t < c.n - 2; t++) {
+        int a = (int)((te >> (9 * t)) & 7), b = (int)((te >> (9 * t + 3)) & 7), d = (int)((te >> (9 * t + 6)) & 7);
+        tri_mask(c.x[a] * u, c.y[a] * u, c.x[b] * u, c.y[b] * u, c.x[d] * u, c.y[d] * u, g.hlo, g.HF, rows);
+    }
+    for (int r = 0; r < g.HF; r++) lut[(size_t)pat * g.HF + r] = rows[r];
+}
+
+cudaError_t build_scale_masks(int s, uint32_t* lut, cudaStream_t st)
+{
+    k_build_scale_masks<<<16, 256, 0, st>>>(s, lut);
+    return cudaGetLastError();
+}
+
+constexpr int kMTW = 32, kMTH = 16;
+constexpr int kMGW = kMTW + 2, kMGH = kMTH + 2, kMGN = kMGW * kMGH;
+constexpr int kMBW = kMTW + 6, kMBH = kMTH + 6;
+constexpr int kMCW = kMTW + 4, kMCH = kMTH + 4;
+
+struct MaskShared {
+    uint8_t graph[kMBH][kMBW];
+    uint32_t pix[kMCH][kMCW];
+    uint8_t spill[kMGN];  // bit e: the polygon reaches into the open square of neighbour e
+    uint8_t live[kMGN];   // the cell exists (inside the image)
+    uint16_t list[kMGN];  // subdivided cells of the tile
+    int count;
+};
+
+__device__ __forceinline__ uint32_t rgba_of(uint32_t p)
+{
+    return ((p >> 16) & 0xFFu) | (p & 0xFF00u) | ((p & 0xFFu) << 16) | 0xFF000000u;
+}
+
+// bit e set when the box [x0,x1]x[y0,y1] (1/64 units) overlaps the open unit
+// square of neighbour e
+__device__ __forceinline__ unsigned spill_bits(int x0, int y0, int x1, int y1)
+{
+    unsigned m = 0;
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        int sx = kUnit * dir_di(e), sy = kUnit * dir_dj(e);
+        if (x1 > sx && x0 < sx + kUnit && y1 > sy && y0 < sy + kUnit) m |= 1u << e;
+    }
+    return m;
+}
+
+template <int LAYOUT, int S>
+__device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
+                                 uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
+                                 int y0)
+{
+    const int s = S > 0 ? S : scale;
+    const MaskGeom G = mask_geom(s);
+    const int F = G.F;
+    // ---- phase A
+    if (threadIdx.x == 0) M.count = 0;
+    for (int k = threadIdx.x; k < kMBW * kMBH; k += blockDim.x) {
+        int gx = x0 - 3 + k % kMBW, gy = y0 - 3 + k / kMBW;
+        unsigned v = 0;
+        if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = __ldg(g + (size_t)gy * w + gx) & inside_mask(gx, gy, w, h);
+        M.graph[k / kMBW][k % kMBW] = (uint8_t)v;
+    }
+    for (int k = threadIdx.x; k < kMCW * kMCH; k += blockDim.x) {
+        int gx = x0 - 2 + k % kMCW, gy = y0 - 2 + k / kMCW;
+        uint32_t v = 0;
+        if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = load_bgr(img, ws, LAYOUT, gx, gy);
+        M.pix[k / kMCW][k % kMCW] = v;
+    }
+    __syncthreads();
+
+    // ---- phase B: plain cells from the table, subdivided cells to the list
+    for (int k = threadIdx.x; k < kMGN; k += blockDim.x) {
+        int lx = k % kMGW, ly = k / kMGW;
+        int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
+        uint32_t* rows = masks + (size_t)k * F;
+        bool live = ci >= 0 && cj >= 0 && ci < w && cj < h;
+        M.live[k] = live;
+        M.spill[k] = 0;
+        if (!live) {
+            for (int r = 0; r < F; r++) rows[r] = 0;
+            continue;
+        }
+        const int bx = lx + 2, by = ly + 2;
+        unsigned node = M.graph[by][bx];
+        if (subdivide && node != 90) {
+            int slot = atomicAdd(&M.count, 1);
+            M.list[slot] = (uint16_t)k;
+            continue;
+        }
+        int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
+        const int dr = G.hlo - G.mlo; // hull window row/column offset inside the footprint
+        const uint32_t* src = lut + (size_t)pat * G.HF;
+        for (int r = 0; r < F; r++) {
+            int q = r - dr;
+            rows[r] = (q >= 0 && q < G.HF) ? (__ldg(src + q) << dr) : 0u;
+        }
+        Poly c;
+        hull_from_lut(__ldg(&g_hull_lut[pat]), c);
+        int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
+        for (int t = 0; t < c.n; t++) {
+            mnx = min(mnx, c.x[t]); mxx = max(mxx, c.x[t]);
+            mny = min(mny, c.y[t]); mxy = max(mxy, c.y[t]);
+        }
+        M.spill[k] = (uint8_t)spill_bits(mnx, mny, mxx, mxy);
+    }
+    __syncthreads();
+
+    // ---- phase B2: subdivided cells, one per thread
+    const int nlist = M.count;
+    for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
+        int k = M.list[q];
+        int lx = k % kMGW, ly = k / kMGW;
+        int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
+        const int bx = lx + 2, by = ly + 2;
+        unsigned node = M.graph[by][bx];
+        int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
+        Poly c, sp;
+        hull_from_lut(__ldg(&g_hull_lut[pat]), c);
+        auto nb_hull = [&](int link, Poly& p) {
+            int nx = bx + dir_di(link), ny = by + dir_dj(link);
+            int np = cell_pattern(M.graph[ny][nx], M.graph[ny][nx - 1], M.graph[ny][nx + 1]);
+            hull_from_lut(__ldg(&g_hull_lut[np]), p);
+        };
+        auto tj = [&](int px, int py) -> bool {
+            long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
+            long long index = (long long)cj * st + (long long)ci * 3;
+            if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
+            if (ci == 0 || ci == w - 1 || cj >= h - 1) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
+            const int qx = lx + 1, qy = ly + 1;
+            auto C = [&](int dx, int dy) { return M.pix[qy + dy][qx + dx]; };
+            if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
+            if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
+            if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
+            if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
+            return false;
+        };
+        subdivide_cell(c, node, nb_hull, tj, sp);
+        uint8_t tri[3 * kMaxPoly];
+        bool ok;
+        int nt = ear_clip(sp, tri, ok);
+        uint32_t* rows = masks + (size_t)k * F;
+        for (int r = 0; r < F; r++) rows[r] = 0;
+        const int u = 4 * s;
+        for (int t = 0; t < nt; t++) {
+            int a = tri[3 * t], b = tri[3 * t + 1], d = tri[3 * t + 2];
+            tri_mask(sp.x[a] * u, sp.y[a] * u, sp.x[b] * u, sp.y[b] * u, sp.x[d] * u, sp.y[d] * u, G.mlo, F, rows);
+        }
+        int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
+        for (int t = 0; t < sp.n; t++) {
+            mnx = min(mnx, sp.x[t]); mxx = max(mxx, sp.x[t]);
+            mny = min(mny, sp.y[t]); mxy = max(mxy, sp.y[t]);
+        }
+        M.spill[k] = nt > 0 ? (uint8_t)spill_bits(mnx, mny, mxx, mxy) : 0;
+    }
+    __syncthreads();
+
+    // ---- phase C: one output block per tile cell
+    const int ow = w * s;
+    const bool vec = ((S == 4 || S == 8) && (ow % 4) == 0 && ((reinterpret_cast<uintptr_t>(out) & 15) == 0));
+    const uint32_t blockbits = (s >= 32) ? 0xFFFFFFFFu : ((1u << s) - 1u);
+    for (int q = threadIdx.x; q < kMTW * kMTH; q += blockDim.x) {
+        int tx = q % kMTW, ty = q / kMTW;
+        int ci = x0 + tx, cj = y0 + ty;
+        if (ci >= w || cj >= h) continue;
+        const int k0 = (ty + 1) * kMGW + (tx + 1);
+        unsigned intr = 0;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            int kn = k0 + dir_dj(e) * kMGW + dir_di(e);
+            intr |= (unsigned)bitof(M.spill[kn], 7 - e);
+        }
+        const uint32_t* own = masks + (size_t)k0 * F;
+        bool full = true;
+        for (int r = 0; r < s; r++) full &= ((own[r - G.mlo] >> (-G.mlo)) & blockbits) == blockbits;
+        const uint32_t own_col = rgba_of(M.pix[ty + 2][tx + 2]);
+        uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
+        if (full && !intr) {
+            for (int r = 0; r < s; r++) {
+                uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
+                if (vec) {
+                    for (int c4 = 0; c4 < s; c4 += 4)
+                        __stcs(reinterpret_cast<uint4*>(o + c4), make_uint4(own_col, own_col, own_col, own_col));
+                } else {
+                    for (int c = 0; c < s; c++) o[c] = own_col;
+                }
+            }
+            continue;
+        }
+        for (int r = 0; r < s; r++) {
+            uint32_t colour[S > 0 ? S : 16];
+            const int ncol = s;
+            uint32_t claimed = 0;
+            uint32_t col_of[9];
+            uint32_t take[9];
+            int qq = 0;
+            for (int dj = 1; dj >= -1; dj--) {
+                int rr = r - s * dj - G.mlo;
+                for (int di = 1; di >= -1; di--, qq++) {
+                    take[qq] = 0;
+                    col_of[qq] = 0;
+                    if (rr < 0 || rr >= F) continue;
+                    int kn = k0 + dj * kMGW + di;
+                    if (!M.live[kn]) continue;
+                    uint64_t wbits = masks[(size_t)kn * F + rr];
+                    int sh = s * di + G.mlo; // block column c = footprint column + sh
+                    uint32_t bits = (uint32_t)((sh >= 0 ? (wbits << sh) : (wbits >> (-sh))) & blockbits);
+                    uint32_t t = bits & ~claimed;
+                    claimed |= t;
+                    take[qq] = t;
+                    col_of[qq] = rgba_of(M.pix[ty + 2 + dj][tx + 2 + di]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < (S > 0 ? S : 16); c++) {
+                if (c >= ncol) break;
+                uint32_t v = 0xFF000000u;
+#pragma unroll
+                for (int z = 0; z < 9; z++)
+                    if ((take[z] >> c) & 1u) v = col_of[z];
+                colour[c] = v;
+            }
+            uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
+            if (vec) {
+#pragma unroll
+                for (int c4 = 0; c4 < (S > 0 ? S : 16); c4 += 4)
+                    if (c4 < ncol)
+                        __stcs(reinterpret_cast<uint4*>(o + c4),
+                               make_uint4(colour[c4], colour[c4 + 1], colour[c4 + 2], colour[c4 + 3]));
+            } else {
+                for (int c = 0; c < ncol; c++) o[c] = colour[c];
+            }
+        }
+    }
+}
+
+template <int LAYOUT, int S>
+__global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32_t* lut)
+{
+    __shared__ MaskShared M;
+    extern __shared__ uint32_t masks[];
+    size_t z = blockIdx.z;
+    mask_raster_tile<LAYOUT, S>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
+                                b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut, blockIdx.x * kMTW,
+                                blockIdx.y * kMTH);
+}
+
+template <int LAYOUT, int S>
+static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
+{
+    MaskGeom g = mask_geom(b.scale);
+    size_t smem = (size_t)kMGN * g.F * sizeof(uint32_t);
+    if (smem > 48 * 1024) {
+        // opt in to more than 48 KB of dynamic shared memory (a per-device
+        // function attribute; setting it again is harmless)
+        cudaError_t e = cudaFuncSetAttribute(k_mask_raster<LAYOUT, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    dim3 grid((b.w + kMTW - 1) / kMTW, (b.h + kMTH - 1) / kMTH, nframes);
+    k_mask_raster<LAYOUT, S><<<grid, 256, smem, s>>>(b, lut);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
+{
+    if (b.layout == DEPIX_LAYOUT_RGBA) {
+        if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4>(b, nframes, lut, s);
+        if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 8>(b, nframes, lut, s);
+        return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0>(b, nframes, lut, s);
+    }
+    if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4>(b, nframes, lut, s);
+    if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 8>(b, nframes, lut, s);
+    return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0>(b, nframes, lut, s);
+}
+
+size_t scale_mask_words(int s) { return (size_t)4096 * mask_geom(s).HF; }
+
 }  // namespace depix

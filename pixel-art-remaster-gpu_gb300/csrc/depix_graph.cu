@@ -253,38 +253,93 @@ __device__ __forceinline__ void uf_unite(int32_t* L, int a, int b)
     }
 }
 
-__global__ void k_cc_init(int32_t* L, int n, size_t frame_stride)
+// Component labels in three passes: union-find inside 32x32 tiles in shared
+// memory (local roots are the tile-local minima, which are also the minima in
+// global index order), then unions across tile borders on the global label
+// array, then one flattening pass.
+constexpr int kLT = 32;
+
+__device__ __forceinline__ int s_find(int* L, int x)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) L[frame_stride * blockIdx.z + k] = k;
+    int p = L[x];
+    while (p != x) {
+        x = p;
+        p = L[x];
+    }
+    return x;
 }
 
-// each node unites with its right, up-right, up and up-left neighbours
-__global__ void k_cc_unite(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+__device__ __forceinline__ void s_unite(int* L, int a, int b)
+{
+    for (;;) {
+        a = s_find(L, a);
+        b = s_find(L, b);
+        if (a == b) return;
+        if (a > b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        int old = atomicMin(&L[b], a);
+        if (old == b) return;
+        b = old;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+{
+    __shared__ int sl[kLT * kLT];
+    __shared__ uint8_t sg[kLT * kLT];
+    g += frame_stride * blockIdx.z;
+    L += frame_stride * blockIdx.z;
+    const int x0 = blockIdx.x * kLT, y0 = blockIdx.y * kLT;
+    for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
+        int x = x0 + p % kLT, y = y0 + p / kLT;
+        sl[p] = p;
+        sg[p] = (x < w && y < h) ? g[(size_t)y * w + x] : 0;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
+        unsigned node = sg[p];
+        if (!node) continue;
+        int lx = p % kLT, ly = p / kLT;
+        int x = x0 + lx, y = y0 + ly;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            if (!bitof(node, e)) continue;
+            int nx = lx + dir_di(e), ny = ly + dir_dj(e);
+            if (nx < 0 || ny < 0 || nx >= kLT || ny >= kLT) continue;
+            if (x + dir_di(e) >= w || y + dir_dj(e) >= h || x + dir_di(e) < 0 || y + dir_dj(e) < 0) continue;
+            s_unite(sl, p, ny * kLT + nx);
+        }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
+        int x = x0 + p % kLT, y = y0 + p / kLT;
+        if (x >= w || y >= h) continue;
+        int r = s_find(sl, p);
+        L[(size_t)y * w + x] = (y0 + r / kLT) * w + (x0 + r % kLT);
+    }
+}
+
+// unions across tile borders: every set bit whose neighbour lies in another
+// tile (each symmetric pair is seen from both ends; uniting twice is harmless)
+__global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= w * h) return;
+    int i = k % w, j = k / w;
+    int ti = i % kLT, tj = j % kLT;
+    if (ti != 0 && ti != kLT - 1 && tj != 0 && tj != kLT - 1) return;
     g += frame_stride * blockIdx.z;
     L += frame_stride * blockIdx.z;
-    int i = k % w, j = k / w;
     unsigned node = g[k];
-    const int dirs[4] = {4, 2, 1, 0};
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        int e = dirs[q];
+    for (int e = 0; e < 8; e++) {
         if (!bitof(node, e)) continue;
         int ni = i + dir_di(e), nj = j + dir_dj(e);
         if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
-        uf_unite(L, k, nj * w + ni);
-    }
-    // a bit set toward a lower neighbour without its mirror still joins the two
-#pragma unroll
-    for (int e = 3; e <= 7; e++) {
-        if (e == 4) continue;
-        if (!bitof(node, e)) continue;
-        int ni = i + dir_di(e), nj = j + dir_dj(e);
-        if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
-        if (bitof(g[nj * w + ni], 7 - e)) continue; // the neighbour's forward edge covers it
+        if (ni / kLT == i / kLT && nj / kLT == j / kLT) continue;
         uf_unite(L, k, nj * w + ni);
     }
 }
@@ -341,9 +396,10 @@ cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int n
                           cudaStream_t s)
 {
     int n = w * h;
+    dim3 tiles((w + kLT - 1) / kLT, (h + kLT - 1) / kLT, nframes);
+    k_cc_local<<<tiles, 256, 0, s>>>(g, labels, w, h, frame_stride);
     dim3 grid((n + 255) / 256, 1, nframes);
-    k_cc_init<<<grid, 256, 0, s>>>(labels, n, frame_stride);
-    k_cc_unite<<<grid, 256, 0, s>>>(g, labels, w, h, frame_stride);
+    k_cc_merge<<<grid, 256, 0, s>>>(g, labels, w, h, frame_stride);
     k_cc_flatten<<<grid, 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }

@@ -80,5 +80,10 @@ cudaError_t launch_triangulate(float* diagram, const int* ec, int w, int h, cuda
 cudaError_t launch_emit(const uint8_t* img, int w, int h, int ws, int layout, const float* diagram, const int* ec,
                         float* pos, uint8_t* col, cudaStream_t s);
 cudaError_t launch_raster(const RasterBatch& b, int nframes, cudaStream_t s);
+// coverage-mask raster (scale <= kMaxMaskScale) and its per-scale pattern table
+constexpr int kMaxMaskScale = 12;
+size_t scale_mask_words(int scale);
+cudaError_t build_scale_masks(int scale, uint32_t* lut, cudaStream_t s);
+cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s);
 
 }  // namespace depix

@@ -216,7 +216,7 @@ def test_sprites_with_transparent_backgrounds(cuda):
         compare(gpu_stages(cuda, img, 48, 1, 1), oracle_all(img, 48, 1))
 
 
-@pytest.mark.parametrize("scale", [1, 2, 3, 8])
+@pytest.mark.parametrize("scale", [1, 2, 3, 5, 8, 12, 13, 16])
 def test_raster_scales(cuda, scale):
     img = synth.frame(21, w=70, h=50)
     g = gpu_stages(cuda, img, 48, 1, 1, scale=scale)
