@@ -815,8 +815,8 @@ static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const
 {
     MaskGeom g = mask_geom(b.scale);
     size_t smem = (size_t)kMGN * g.F * sizeof(uint32_t);
-    if (smem > 48 * 1024) {
-        // opt in to more than 48 KB of dynamic shared memory (a per-device
+    if (smem + sizeof(MaskShared) > 48 * 1024) {
+        // opt in to more than 48 KB of shared memory in total (a per-device
         // function attribute; setting it again is harmless)
         cudaError_t e = cudaFuncSetAttribute(k_mask_raster<LAYOUT, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
