@@ -25,6 +25,17 @@ __host__ __device__ __forceinline__ int dir_di(int e) { return ((0x9224 >> (2 * 
 __host__ __device__ __forceinline__ int dir_dj(int e) { return ((0x016A >> (2 * e)) & 3) - 1; }
 __host__ __device__ __forceinline__ int bitof(unsigned v, int k) { return (int)((v >> k) & 1u); }
 
+// bits of a node whose neighbour lies inside the image
+__device__ __forceinline__ unsigned inside_mask(int x, int y, int w, int h)
+{
+    unsigned m = 0xFFu;
+    if (x == 0) m &= ~0x29u;     // 0, 3, 5
+    if (x == w - 1) m &= ~0x94u; // 2, 4, 7
+    if (y == 0) m &= ~0xE0u;     // 5, 6, 7
+    if (y == h - 1) m &= ~0x07u; // 0, 1, 2
+    return m;
+}
+
 // ------------------------------------------------------------------ colour
 
 // Packed Y/U/V word of one pixel from its bytes in the reference's memory
@@ -141,11 +152,14 @@ __device__ __forceinline__ int cell_pattern(unsigned node, unsigned left, unsign
            (bitof(right, 5) << 11);
 }
 
-// A cell polygon in 1/64-cell units.
+// A cell polygon in 1/64-cell units. Every vertex lies in [-0.75, 1.75] of
+// its cell (hull points in [-0.25, 1.25]; subdivision midpoints pair an own
+// point with a neighbour's), i.e. in [-48, 112]: int8 storage keeps the
+// per-thread arrays small.
 struct Poly {
     int n;
-    int x[kMaxPoly];
-    int y[kMaxPoly];
+    int8_t x[kMaxPoly];
+    int8_t y[kMaxPoly];
 };
 
 // Decodes a hull table entry (built once per device in depix_geom.cu):
@@ -157,8 +171,8 @@ __device__ __forceinline__ void hull_from_lut(uint64_t e, Poly& p)
 #pragma unroll
     for (int t = 0; t < kMaxHull; t++) {
         unsigned v = (unsigned)(e >> (4 + 6 * t)) & 63u;
-        p.x[t] = ((int)(v & 7) - 1) * (kUnit / 4);
-        p.y[t] = ((int)(v >> 3) - 1) * (kUnit / 4);
+        p.x[t] = (int8_t)(((int)(v & 7) - 1) * (kUnit / 4));
+        p.y[t] = (int8_t)(((int)(v >> 3) - 1) * (kUnit / 4));
     }
 }
 
@@ -239,30 +253,30 @@ __device__ void subdivide_cell(const Poly& c, unsigned node, NbHull nb_hull, TJ 
             // the test's image-bounds check answers "keep" for any vertex of
             // the cells it covers, before it looks at corners
             if (tj(px, py)) {
-                out.x[m] = px; out.y[m] = py; m++;
+                out.x[m] = (int8_t)px; out.y[m] = (int8_t)py; m++;
             } else {
                 int rx, ry, qx, qy;
                 qr_point(c, v - 1, true, rx, ry);
                 qr_point(c, v, false, qx, qy);
-                out.x[m] = rx; out.y[m] = ry; m++;
-                out.x[m] = qx; out.y[m] = qy; m++;
+                out.x[m] = (int8_t)rx; out.y[m] = (int8_t)ry; m++;
+                out.x[m] = (int8_t)qx; out.y[m] = (int8_t)qy; m++;
             }
         } else if (!cur && prev) {
             int qx, qy, ax, ay;
             qr_point(c, v, false, qx, qy);
             nb_hull(lp, nb);
             linked_point(nb, lp, px, py, true, ax, ay);
-            out.x[m] = (qx + ax) / 2; out.y[m] = (qy + ay) / 2; m++;
-            out.x[m] = qx; out.y[m] = qy; m++;
+            out.x[m] = (int8_t)((qx + ax) / 2); out.y[m] = (int8_t)((qy + ay) / 2); m++;
+            out.x[m] = (int8_t)qx; out.y[m] = (int8_t)qy; m++;
         } else if (cur && !prev) {
             int rx, ry, ax, ay;
             nb_hull(link[v], nb);
             linked_point(nb, link[v], px, py, false, ax, ay);
             qr_point(c, v - 1, true, rx, ry);
-            out.x[m] = rx; out.y[m] = ry; m++;
-            out.x[m] = (rx + ax) / 2; out.y[m] = (ry + ay) / 2; m++;
+            out.x[m] = (int8_t)rx; out.y[m] = (int8_t)ry; m++;
+            out.x[m] = (int8_t)((rx + ax) / 2); out.y[m] = (int8_t)((ry + ay) / 2); m++;
         } else {
-            out.x[m] = px; out.y[m] = py; m++;
+            out.x[m] = (int8_t)px; out.y[m] = (int8_t)py; m++;
         }
     }
     out.n = m;
@@ -289,8 +303,8 @@ __device__ __forceinline__ int ear_clip(const Poly& c, uint8_t* tri, bool& ok)
     if (n < 3) { ok = false; return 0; }
     int area = 0;
     for (int p = n - 1, q = 0; q < n; p = q++) area += c.x[p] * c.y[q] - c.x[q] * c.y[p];
-    int V[kMaxPoly];
-    for (int v = 0; v < n; v++) V[v] = area > 0 ? v : (n - 1) - v;
+    uint8_t V[kMaxPoly];
+    for (int v = 0; v < n; v++) V[v] = (uint8_t)(area > 0 ? v : (n - 1) - v);
     int nv = n, nt = 0, count = 2 * nv;
     for (int v = nv - 1; nv > 2;) {
         if (0 >= (count--)) { ok = false; return nt; }
@@ -302,11 +316,17 @@ __device__ __forceinline__ int ear_clip(const Poly& c, uint8_t* tri, bool& ok)
         if (nv <= w) w = 0;
         int Ax = c.x[V[u]], Ay = c.y[V[u]], Bx = c.x[V[v]], By = c.y[V[v]], Cx = c.x[V[w]], Cy = c.y[V[w]];
         bool ear = ((Bx - Ax) * (Cy - Ay) - (By - Ay) * (Cx - Ax)) > 0;
-        if (ear)
+        if (ear) {
+            // a point outside the triangle's bounding box cannot be inside or on it
+            const int x0 = min(Ax, min(Bx, Cx)), x1 = max(Ax, max(Bx, Cx));
+            const int y0 = min(Ay, min(By, Cy)), y1 = max(Ay, max(By, Cy));
             for (int p = 0; p < nv; p++) {
                 if (p == u || p == v || p == w) continue;
-                if (inside_tri(Ax, Ay, Bx, By, Cx, Cy, c.x[V[p]], c.y[V[p]])) { ear = false; break; }
+                const int Px = c.x[V[p]], Py = c.y[V[p]];
+                if (Px < x0 || Px > x1 || Py < y0 || Py > y1) continue;
+                if (inside_tri(Ax, Ay, Bx, By, Cx, Cy, Px, Py)) { ear = false; break; }
             }
+        }
         if (ear) {
             tri[3 * nt] = (uint8_t)V[u];
             tri[3 * nt + 1] = (uint8_t)V[v];

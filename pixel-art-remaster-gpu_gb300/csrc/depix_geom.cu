@@ -186,8 +186,8 @@ __device__ __forceinline__ bool poly_from_slots(const float2* cell, int n, int c
     p.n = n;
     for (int t = 0; t < n; t++) {
         float2 v = cell[t];
-        p.x[t] = __float2int_rn(v.x * (float)kUnit);
-        p.y[t] = __float2int_rn(v.y * (float)kUnit);
+        p.x[t] = (int8_t)__float2int_rn(v.x * (float)kUnit);
+        p.y[t] = (int8_t)__float2int_rn(v.y * (float)kUnit);
     }
     return true;
 }
@@ -318,16 +318,6 @@ struct RasterShared {
     int8_t bb[kGN][4];
 };
 
-// bits of a node whose neighbour lies inside the image
-__device__ __forceinline__ unsigned inside_mask(int x, int y, int w, int h)
-{
-    unsigned m = 0xFFu;
-    if (x == 0) m &= ~0x29u;     // 0, 3, 5
-    if (x == w - 1) m &= ~0x94u; // 2, 4, 7
-    if (y == 0) m &= ~0xE0u;     // 5, 6, 7
-    if (y == h - 1) m &= ~0x07u; // 0, 1, 2
-    return m;
-}
 
 template <int LAYOUT>
 __device__ void raster_tile(RasterShared& S, const uint8_t* img, int ws, const uint8_t* g, uint8_t* out, int w,
@@ -394,8 +384,8 @@ __device__ void raster_tile(RasterShared& S, const uint8_t* img, int ws, const u
         }
         int mnx = 127, mny = 127, mxx = -128, mxy = -128;
         for (int t = 0; t < c.n; t++) {
-            S.vx[k][t] = (int8_t)c.x[t];
-            S.vy[k][t] = (int8_t)c.y[t];
+            S.vx[k][t] = c.x[t];
+            S.vy[k][t] = c.y[t];
             mnx = min(mnx, c.x[t]); mxx = max(mxx, c.x[t]);
             mny = min(mny, c.y[t]); mxy = max(mxy, c.y[t]);
         }

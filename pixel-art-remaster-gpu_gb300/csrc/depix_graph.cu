@@ -256,17 +256,23 @@ __device__ __forceinline__ void uf_unite(int32_t* L, int a, int b)
 // Component labels in three passes: union-find inside 32x32 tiles in shared
 // memory (local roots are the tile-local minima, which are also the minima in
 // global index order), then unions across tile borders on the global label
-// array, then one flattening pass.
+// array, then one flattening pass. Inside a tile a warp owns a row: horizontal
+// runs come from one ballot (a run's root is its leftmost pixel), and rows
+// are joined with one union per pair of touching runs.
 constexpr int kLT = 32;
 
+// find with path compression; parents only ever decrease, so lowering a
+// parent to the root found is safe under concurrent unions
 __device__ __forceinline__ int s_find(int* L, int x)
 {
-    int p = L[x];
-    while (p != x) {
-        x = p;
-        p = L[x];
+    int r = x;
+    while (L[r] != r) r = L[r];
+    while (L[x] > r) {
+        int nx = L[x];
+        atomicMin(&L[x], r);
+        x = nx;
     }
-    return x;
+    return r;
 }
 
 __device__ __forceinline__ void s_unite(int* L, int a, int b)
@@ -289,28 +295,41 @@ __device__ __forceinline__ void s_unite(int* L, int a, int b)
 __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
 {
     __shared__ int sl[kLT * kLT];
+    __shared__ uint16_t run[kLT * kLT];
     __shared__ uint8_t sg[kLT * kLT];
     g += frame_stride * blockIdx.z;
     L += frame_stride * blockIdx.z;
     const int x0 = blockIdx.x * kLT, y0 = blockIdx.y * kLT;
     for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
         int x = x0 + p % kLT, y = y0 + p / kLT;
-        sl[p] = p;
-        sg[p] = (x < w && y < h) ? g[(size_t)y * w + x] : 0;
+        sg[p] = (x < w && y < h) ? g[(size_t)y * w + x] & inside_mask(x, y, w, h) : 0;
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int r = warp; r < kLT; r += nwarp) {
+        int p = r * kLT + lane;
+        bool link = lane > 0 && (bitof(sg[p], 3) || bitof(sg[p - 1], 4));
+        unsigned starts = __ballot_sync(0xFFFFFFFFu, !link);
+        unsigned upto = lane == 31 ? starts : (starts & ((2u << lane) - 1u));
+        int root = r * kLT + (31 - __clz(upto));
+        run[p] = (uint16_t)root;
+        sl[p] = root;
+    }
+    __syncthreads();
+    for (int r = warp; r < kLT - 1; r += nwarp) {
+        int p = r * kLT + lane;
         unsigned node = sg[p];
-        if (!node) continue;
-        int lx = p % kLT, ly = p / kLT;
-        int x = x0 + lx, y = y0 + ly;
 #pragma unroll
-        for (int e = 0; e < 8; e++) {
-            if (!bitof(node, e)) continue;
-            int nx = lx + dir_di(e), ny = ly + dir_dj(e);
-            if (nx < 0 || ny < 0 || nx >= kLT || ny >= kLT) continue;
-            if (x + dir_di(e) >= w || y + dir_dj(e) >= h || x + dir_di(e) < 0 || y + dir_dj(e) < 0) continue;
-            s_unite(sl, p, ny * kLT + nx);
+        for (int e = 0; e <= 2; e++) { // up-left, up, up-right
+            int nl = lane + dir_di(e);
+            if (nl < 0 || nl >= kLT) continue;
+            int q = p + kLT + dir_di(e);
+            if (!(bitof(node, e) || bitof(sg[q], 7 - e))) continue;
+            // the lane to the left already joins the same two runs
+            if (lane > 0 && nl > 0 && run[p - 1] == run[p] && run[q - 1] == run[q] &&
+                (bitof(sg[p - 1], e) || bitof(sg[q - 1], 7 - e)))
+                continue;
+            s_unite(sl, run[p], run[q]);
         }
     }
     __syncthreads();
