@@ -228,14 +228,15 @@ def run_ours(args, rank, world, local_rank):
     frames_total = B * args.steps * world
     value = frames_total / (ms / 1e3)
 
-    # roofline of the dominant kernel (raster stage: one kernel per call)
+    # roofline of the kernel that writes the output (the raster stage: one
+    # kernel per call); algorithmic bytes: image and graph in, raster out
     r_ms, r_launches, r_calls = stages["raster"]
     raster_ms = r_ms / max(r_calls, 1)
     alg_bytes = B * (W * H * 4 + W * H * 1 + out_px * 4)
     achieved = alg_bytes / (raster_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     tpf = profiled_traffic()
-    roofline = {"kernel": "k_raster (cells + subdivision + ear clip + raster, fused)", "bound": "hbm",
+    roofline = {"kernel": "k_mask_raster (cell masks, block resolution, 16-byte output stores)", "bound": "hbm",
                 "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (tpf * B if tpf else None),
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": round(raster_ms, 4),

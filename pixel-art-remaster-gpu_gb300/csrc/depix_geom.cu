@@ -508,7 +508,7 @@ __host__ __device__ __forceinline__ MaskGeom mask_geom(int s)
 // triangle covers under the top-left rule. Vertices in 1/256 output pixel
 // relative to the cell origin.
 __device__ __forceinline__ void tri_mask(int ax, int ay, int bx, int by, int cx, int cy, int mlo, int F,
-                                         uint32_t* rows)
+                                         uint32_t* rows, int rstride = 1)
 {
     int area = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
     if (area == 0) return;
@@ -539,7 +539,7 @@ __device__ __forceinline__ void tri_mask(int ax, int ay, int bx, int by, int cx,
             int px = 256 * m + 128;
             if (A0 * px + e0 >= b0 && A1 * px + e1 >= b1 && A2 * px + e2 >= b2) bits |= 1u << (m - mlo);
         }
-        rows[n - mlo] |= bits;
+        if (bits) rows[(n - mlo) * rstride] |= bits;
     }
 }
 
@@ -600,10 +600,125 @@ __device__ __forceinline__ unsigned spill_bits(int x0, int y0, int x1, int y1)
     return m;
 }
 
+// Footprint mask rows (F words at rows[r * rstride]) and spill bits of one
+// subdivided cell: corner cutting against the linked neighbours' hulls, the
+// reference's ear clip, then the triangles' coverage. G(dx, dy) is the graph
+// byte of the cell at that offset (0 outside the image, bits toward outside
+// cleared); TJ(px, py) the corner test.
+template <typename GraphAt, typename TJ>
+__device__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint32_t* rows, int rstride)
+{
+    unsigned node = G(0, 0);
+    int pat = cell_pattern(node, G(-1, 0), G(1, 0));
+    Poly c, sp;
+    hull_from_lut(__ldg(&g_hull_lut[pat]), c);
+    auto nb_hull = [&](int link, Poly& p) {
+        int dx = dir_di(link), dy = dir_dj(link);
+        int np = cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy));
+        hull_from_lut(__ldg(&g_hull_lut[np]), p);
+    };
+    subdivide_cell(c, node, nb_hull, tj, sp);
+    uint8_t tri[3 * kMaxPoly];
+    bool ok;
+    int nt = ear_clip(sp, tri, ok);
+    for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
+    const int u = 4 * Gm.s;
+    for (int t = 0; t < nt; t++) {
+        int a = tri[3 * t], b = tri[3 * t + 1], d = tri[3 * t + 2];
+        tri_mask(sp.x[a] * u, sp.y[a] * u, sp.x[b] * u, sp.y[b] * u, sp.x[d] * u, sp.y[d] * u, Gm.mlo, Gm.F, rows,
+                 rstride);
+    }
+    if (nt == 0) return 0;
+    int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
+    for (int t = 0; t < sp.n; t++) {
+        mnx = min(mnx, (int)sp.x[t]); mxx = max(mxx, (int)sp.x[t]);
+        mny = min(mny, (int)sp.y[t]); mxy = max(mxy, (int)sp.y[t]);
+    }
+    return spill_bits(mnx, mny, mxx, mxy);
+}
+
+int complex_mask_words(int scale) { return mask_geom(scale).F + 1; }
+
+// Subdivided-cell masks for whole frames. Each warp scans 256 consecutive
+// cells 32 at a time, queues the subdivided ones with a ballot and works them
+// off 32 at a time, so every lane has a cell and nothing waits on the block.
+constexpr int kCxWarpCells = 256;
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) k_complex_masks(RasterBatch b)
+{
+    __shared__ int queue[8][64];
+    __shared__ uint32_t rows_s[32 * 256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t z = blockIdx.z;
+    const uint8_t* img = b.img + b.img_stride * z;
+    const uint8_t* g = b.graph + b.graph_stride * z;
+    uint32_t* cm = b.cmask + b.cmask_stride * z;
+    const int w = b.w, h = b.h, ws = b.ws, n = w * h;
+    const MaskGeom Gm = mask_geom(b.scale);
+    const int words = Gm.F + 1;
+    uint32_t* rows = rows_s + threadIdx.x;
+
+    auto process = [&](int cell) {
+        const int ci = cell % w, cj = cell / w;
+        auto G = [&](int dx, int dy) -> unsigned {
+            int x = ci + dx, y = cj + dy;
+            if (x < 0 || y < 0 || x >= w || y >= h) return 0u;
+            return __ldg(g + (size_t)y * w + x) & inside_mask(x, y, w, h);
+        };
+        auto tj = [&](int px, int py) -> bool {
+            long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
+            long long index = (long long)cj * st + (long long)ci * 3;
+            if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
+            if (ci == 0 || ci == w - 1 || cj >= h - 1) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
+            auto C = [&](int dx, int dy) { return load_bgr(img, ws, LAYOUT, ci + dx, cj + dy); };
+            if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
+            if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
+            if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
+            if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
+            return false;
+        };
+        unsigned spill = complex_cell_mask(G, tj, Gm, rows, 256);
+        uint32_t* o = cm + (size_t)cell * words;
+        for (int r = 0; r < Gm.F; r++) o[r] = rows[r * 256];
+        o[Gm.F] = spill;
+    };
+
+    const int base = blockIdx.x * (8 * kCxWarpCells) + warp * kCxWarpCells;
+    int qn = 0;
+    for (int r = 0; r < kCxWarpCells / 32; r++) {
+        int cell = base + r * 32 + lane;
+        bool cx = cell < n && g[cell] != 90;
+        unsigned bal = __ballot_sync(0xFFFFFFFFu, cx);
+        if (cx) queue[warp][qn + __popc(bal & ((1u << lane) - 1u))] = cell;
+        qn += __popc(bal);
+        __syncwarp();
+        if (qn >= 32) {
+            process(queue[warp][lane]);
+            __syncwarp();
+            if (lane < qn - 32) queue[warp][lane] = queue[warp][lane + 32];
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (lane < qn) process(queue[warp][lane]);
+}
+
+cudaError_t launch_complex_masks(const RasterBatch& b, int nframes, cudaStream_t s)
+{
+    int n = b.w * b.h;
+    dim3 grid((n + 8 * kCxWarpCells - 1) / (8 * kCxWarpCells), 1, nframes);
+    if (b.layout == DEPIX_LAYOUT_RGBA)
+        k_complex_masks<DEPIX_LAYOUT_RGBA><<<grid, 256, 0, s>>>(b);
+    else
+        k_complex_masks<DEPIX_LAYOUT_BGR><<<grid, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
 template <int LAYOUT, int S>
 __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
-                                 uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
-                                 int y0)
+                                 uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut,
+                                 const uint32_t* cmask, int x0, int y0)
 {
     const int s = S > 0 ? S : scale;
     const MaskGeom G = mask_geom(s);
@@ -639,8 +754,14 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
         const int bx = lx + 2, by = ly + 2;
         unsigned node = M.graph[by][bx];
         if (subdivide && node != 90) {
-            int slot = atomicAdd(&M.count, 1);
-            M.list[slot] = (uint16_t)k;
+            if (cmask) {
+                const uint32_t* src = cmask + ((size_t)cj * w + ci) * (F + 1);
+                for (int r = 0; r < F; r++) rows[r] = __ldg(src + r);
+                M.spill[k] = (uint8_t)__ldg(src + F);
+            } else {
+                int slot = atomicAdd(&M.count, 1);
+                M.list[slot] = (uint16_t)k;
+            }
             continue;
         }
         int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
@@ -661,22 +782,14 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
     }
     __syncthreads();
 
-    // ---- phase B2: subdivided cells, one per thread
+    // ---- phase B2: subdivided cells, one per thread (when not precomputed)
     const int nlist = M.count;
     for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
         int k = M.list[q];
         int lx = k % kMGW, ly = k / kMGW;
         int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
         const int bx = lx + 2, by = ly + 2;
-        unsigned node = M.graph[by][bx];
-        int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
-        Poly c, sp;
-        hull_from_lut(__ldg(&g_hull_lut[pat]), c);
-        auto nb_hull = [&](int link, Poly& p) {
-            int nx = bx + dir_di(link), ny = by + dir_dj(link);
-            int np = cell_pattern(M.graph[ny][nx], M.graph[ny][nx - 1], M.graph[ny][nx + 1]);
-            hull_from_lut(__ldg(&g_hull_lut[np]), p);
-        };
+        auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx]; };
         auto tj = [&](int px, int py) -> bool {
             long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
             long long index = (long long)cj * st + (long long)ci * 3;
@@ -690,23 +803,7 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
             if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
             return false;
         };
-        subdivide_cell(c, node, nb_hull, tj, sp);
-        uint8_t tri[3 * kMaxPoly];
-        bool ok;
-        int nt = ear_clip(sp, tri, ok);
-        uint32_t* rows = masks + (size_t)k * F;
-        for (int r = 0; r < F; r++) rows[r] = 0;
-        const int u = 4 * s;
-        for (int t = 0; t < nt; t++) {
-            int a = tri[3 * t], b = tri[3 * t + 1], d = tri[3 * t + 2];
-            tri_mask(sp.x[a] * u, sp.y[a] * u, sp.x[b] * u, sp.y[b] * u, sp.x[d] * u, sp.y[d] * u, G.mlo, F, rows);
-        }
-        int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
-        for (int t = 0; t < sp.n; t++) {
-            mnx = min(mnx, sp.x[t]); mxx = max(mxx, sp.x[t]);
-            mny = min(mny, sp.y[t]); mxy = max(mxy, sp.y[t]);
-        }
-        M.spill[k] = nt > 0 ? (uint8_t)spill_bits(mnx, mny, mxx, mxy) : 0;
+        M.spill[k] = (uint8_t)complex_cell_mask(Gs, tj, G, masks + (size_t)k * F, 1);
     }
     __syncthreads();
 
@@ -796,8 +893,8 @@ __global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32
     extern __shared__ uint32_t masks[];
     size_t z = blockIdx.z;
     mask_raster_tile<LAYOUT, S>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
-                                b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut, blockIdx.x * kMTW,
-                                blockIdx.y * kMTH);
+                                b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut,
+                                b.cmask ? b.cmask + b.cmask_stride * z : nullptr, blockIdx.x * kMTW, blockIdx.y * kMTH);
 }
 
 template <int LAYOUT, int S>
