@@ -364,3 +364,305 @@ __device__ __forceinline__ bool covers(int ax, int ay, int bx, int by, int cx, i
 }
 
 }  // namespace depix
+
+namespace depix {
+
+// ------------------------------------------- register-packed cell geometry
+//
+// The mask path keeps a cell's geometry in registers: a hull as its 64-bit
+// pattern-table entry, a cut polygon as 16 signed-byte coordinates per axis in
+// two 64-bit words. Same decisions as the Poly-based functions above.
+
+struct Packed {
+    uint64_t x0, x1, y0, y1; // vertex t: byte (t & 7) of (t < 8 ? *0 : *1)
+    int n;
+};
+
+__device__ __forceinline__ int pk_get(uint64_t lo, uint64_t hi, int t)
+{
+    uint64_t w = t < 8 ? lo : hi;
+    return (int)(int8_t)(uint8_t)(w >> ((t & 7) * 8));
+}
+
+__device__ __forceinline__ void pk_put(Packed& P, int t, int x, int y)
+{
+    const int sh = (t & 7) * 8;
+    const uint64_t keep = ~(0xFFull << sh);
+    const uint64_t bx = (uint64_t)(uint8_t)x << sh, by = (uint64_t)(uint8_t)y << sh;
+    if (t < 8) {
+        P.x0 = (P.x0 & keep) | bx;
+        P.y0 = (P.y0 & keep) | by;
+    } else {
+        P.x1 = (P.x1 & keep) | bx;
+        P.y1 = (P.y1 & keep) | by;
+    }
+}
+
+// hull vertex t of a pattern-table entry, in 1/64 cell
+__device__ __forceinline__ int hx(uint64_t e, int t) { return ((int)((e >> (4 + 6 * t)) & 7u) - 1) * (kUnit / 4); }
+__device__ __forceinline__ int hy(uint64_t e, int t) { return ((int)((e >> (7 + 6 * t)) & 7u) - 1) * (kUnit / 4); }
+
+// edge_link (isLinkedEdge) on a hull entry
+__device__ __forceinline__ int hull_edge_link(uint64_t e, int n, unsigned node, int idx)
+{
+    int b = idx + 1 == n ? 0 : idx + 1;
+    int ax = hx(e, idx), ay = hy(e, idx), bx = hx(e, b), by = hy(e, b);
+    int dx = bx - ax, dy = by - ay, my2 = ay + by;
+    const int half = kUnit / 2;
+    if (ay == by && ay > half && bitof(node, 1)) return 1;
+    if (ax == bx && ax > half && bitof(node, 4)) return 4;
+    if (ay == by && ay < half && bitof(node, 6)) return 6;
+    if (ax == bx && ax < half && bitof(node, 3)) return 3;
+    bool s1 = dx != 0 && dy == dx, sm1 = dx != 0 && dy == -dx;
+    if (s1 && my2 > kUnit && bitof(node, 0)) return 0;
+    if (sm1 && my2 > kUnit && bitof(node, 2)) return 2;
+    if (s1 && my2 < kUnit && bitof(node, 7)) return 7;
+    if (sm1 && my2 < kUnit && bitof(node, 5)) return 5;
+    return -1;
+}
+
+// getQ_i / getR_i on a hull entry (index i taken modulo n, as the reference)
+__device__ __forceinline__ void hull_qr(uint64_t e, int n, int i, bool want_r, int& ox, int& oy)
+{
+    int a = i % n;
+    if (a < 0) a += n;
+    int b = (i + 1) % n;
+    int px = hx(e, a), py = hy(e, a), nx = hx(e, b), ny = hy(e, b);
+    int l2 = (nx - px) * (nx - px) + (ny - py) * (ny - py);
+    int wp, wn, d;
+    if (l2 <= kUnit * kUnit) {
+        wp = want_r ? 1 : 3;
+        wn = want_r ? 3 : 1;
+        d = 4;
+    } else {
+        wp = want_r ? 1 : 7;
+        wn = want_r ? 7 : 1;
+        d = 8;
+    }
+    ox = (wp * px + wn * nx) / d;
+    oy = (wp * py + wn * ny) / d;
+}
+
+// One corner-cutting round on a hull entry into a packed polygon
+// (subdivision, subdivision_functions.cu:564-669). NbEntry(link) returns the
+// pattern-table entry of the neighbour in that direction; TJ(px, py) is the
+// corner test.
+template <typename NbEntry, typename TJ>
+__device__ __forceinline__ void subdivide_packed(uint64_t e, unsigned node, NbEntry nb_entry, TJ tj, Packed& out)
+{
+    const int n = (int)(e & 0xF);
+    uint32_t links = 0; // 4 bits per edge: link direction, 15 = border
+    for (int v = 0; v < n; v++) links |= (uint32_t)(hull_edge_link(e, n, node, v) & 15) << (4 * v);
+    out.x0 = out.x1 = out.y0 = out.y1 = 0;
+    int m = 0;
+    for (int v = 0; v < n; v++) {
+        const int lc = (int)((links >> (4 * v)) & 15u);
+        const int lp = (int)((links >> (4 * (v == 0 ? n - 1 : v - 1))) & 15u);
+        const bool cur = lc != 15, prev = lp != 15;
+        const int px = hx(e, v), py = hy(e, v);
+        int qx, qy, rx, ry;
+        hull_qr(e, n, v, false, qx, qy);
+        hull_qr(e, n, v - 1, true, rx, ry);
+        if (cur == prev) {
+            if (cur || tj(px, py)) {
+                pk_put(out, m++, px, py);
+            } else {
+                pk_put(out, m++, rx, ry);
+                pk_put(out, m++, qx, qy);
+            }
+            continue;
+        }
+        // exactly one adjacent edge is linked: the neighbour's R (previous
+        // edge linked) or Q (current edge linked) around the matching vertex
+        const int L = prev ? lp : lc;
+        const uint64_t ne = nb_entry(L);
+        const int nn = (int)(ne & 0xF);
+        const int tx = px - kUnit * dir_di(L), ty = py - kUnit * dir_dj(L);
+        int op = 0;
+        for (int t = 0; t < nn; t++)
+            if (hx(ne, t) == tx && hy(ne, t) == ty) {
+                op = t;
+                break;
+            }
+        int ax, ay;
+        hull_qr(ne, nn, prev ? op - 1 : op, prev, ax, ay);
+        ax += kUnit * dir_di(L);
+        ay += kUnit * dir_dj(L);
+        if (prev) { // current edge border: mid(Q, R_adjacent), Q
+            pk_put(out, m++, (qx + ax) / 2, (qy + ay) / 2);
+            pk_put(out, m++, qx, qy);
+        } else { // current edge linked: R, mid(R, Q_adjacent)
+            pk_put(out, m++, rx, ry);
+            pk_put(out, m++, (rx + ax) / 2, (ry + ay) / 2);
+        }
+    }
+    out.n = m;
+}
+
+// bit k set where byte k of m is 0xFF (m from a per-byte SIMD compare)
+__device__ __forceinline__ unsigned byte_bits(uint32_t m) { return (((m >> 7) & 0x01010101u) * 0x10204080u) >> 28; }
+
+// vertices (bit t) whose point lies in [x0,x1] x [y0,y1]
+__device__ __forceinline__ unsigned in_box16(const Packed& P, int x0, int x1, int y0, int y1)
+{
+    const uint32_t bx0 = (uint8_t)x0 * 0x01010101u, bx1 = (uint8_t)x1 * 0x01010101u;
+    const uint32_t by0 = (uint8_t)y0 * 0x01010101u, by1 = (uint8_t)y1 * 0x01010101u;
+    unsigned m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t xw = (uint32_t)((k < 2 ? P.x0 : P.x1) >> (32 * (k & 1)));
+        uint32_t yw = (uint32_t)((k < 2 ? P.y0 : P.y1) >> (32 * (k & 1)));
+        uint32_t in = __vcmpges4(xw, bx0) & __vcmples4(xw, bx1) & __vcmpges4(yw, by0) & __vcmples4(yw, by1);
+        m |= byte_bits(in) << (4 * k);
+    }
+    return m;
+}
+
+}  // namespace depix
+
+namespace depix {
+
+// Ear clipping (process / snip / area, triangulate_functions.cu:6-217) on a
+// packed polygon. Index list V as 4-bit entries of one word; the inside test
+// runs only for the vertices in the ear's bounding box (a vertex outside it
+// cannot be inside or on the triangle). Each ear goes to on_tri(A, B, C) as
+// it is found. Returns the ear count; ok = false when the reference's loop
+// guard gives up.
+template <typename OnTri>
+__device__ __forceinline__ int ear_clip_packed(const Packed& P, OnTri on_tri, bool& ok)
+{
+    ok = true;
+    const int n = P.n;
+    if (n < 3) {
+        ok = false;
+        return 0;
+    }
+    int area = 0;
+    for (int p = n - 1, q = 0; q < n; p = q++)
+        area += pk_get(P.x0, P.x1, p) * pk_get(P.y0, P.y1, q) - pk_get(P.x0, P.x1, q) * pk_get(P.y0, P.y1, p);
+    uint64_t V = 0;
+    for (int v = 0; v < n; v++) V |= (uint64_t)(area > 0 ? v : n - 1 - v) << (4 * v);
+    unsigned alive = (1u << n) - 1u;
+    int nv = n, nt = 0, count = 2 * nv;
+    for (int v = nv - 1; nv > 2;) {
+        if (0 >= (count--)) {
+            ok = false;
+            return nt;
+        }
+        int u = v;
+        if (nv <= u) u = 0;
+        v = u + 1;
+        if (nv <= v) v = 0;
+        int w = v + 1;
+        if (nv <= w) w = 0;
+        const int A = (int)((V >> (4 * u)) & 15u), B = (int)((V >> (4 * v)) & 15u), C = (int)((V >> (4 * w)) & 15u);
+        const int Ax = pk_get(P.x0, P.x1, A), Ay = pk_get(P.y0, P.y1, A);
+        const int Bx = pk_get(P.x0, P.x1, B), By = pk_get(P.y0, P.y1, B);
+        const int Cx = pk_get(P.x0, P.x1, C), Cy = pk_get(P.y0, P.y1, C);
+        bool ear = ((Bx - Ax) * (Cy - Ay) - (By - Ay) * (Cx - Ax)) > 0;
+        if (ear) {
+            unsigned cand = alive & ~((1u << A) | (1u << B) | (1u << C)) &
+                            in_box16(P, min(Ax, min(Bx, Cx)), max(Ax, max(Bx, Cx)), min(Ay, min(By, Cy)),
+                                     max(Ay, max(By, Cy)));
+            while (cand) {
+                const int p = __ffs(cand) - 1;
+                cand &= cand - 1u;
+                if (inside_tri(Ax, Ay, Bx, By, Cx, Cy, pk_get(P.x0, P.x1, p), pk_get(P.y0, P.y1, p))) {
+                    ear = false;
+                    break;
+                }
+            }
+        }
+        if (ear) {
+            on_tri(Ax, Ay, Bx, By, Cx, Cy);
+            nt++;
+            const uint64_t low = (1ull << (4 * v)) - 1ull;
+            V = (V & low) | ((V >> 4) & ~low);
+            alive &= ~(1u << B);
+            nv--;
+            count = 2 * nv;
+        }
+    }
+    return nt;
+}
+
+}  // namespace depix
+
+namespace depix {
+
+__device__ __forceinline__ int floor_div(int a, int b) // b > 0
+{
+    int q = a / b;
+    return (a % b != 0 && a < 0) ? q - 1 : q;
+}
+
+// True when every edge turns strictly counter-clockwise around the cell
+// centre (32, 32) and the polygon winds around it exactly once: the vertices
+// are then in increasing angle around the centre, so the polygon is
+// star-shaped about it, hence simple. For a simple polygon the reference's
+// ear clip never gives up (every position is tried within nv attempts and a
+// simple polygon always has an ear its test accepts) and its triangles tile
+// the polygon exactly.
+__device__ __forceinline__ bool star_simple(const Packed& P)
+{
+    const int n = P.n;
+    if (n < 3) return false;
+    int px = pk_get(P.x0, P.x1, n - 1) - kUnit / 2, py = pk_get(P.y0, P.y1, n - 1) - kUnit / 2;
+    int wraps = 0;
+    for (int i = 0; i < n; i++) {
+        const int x = pk_get(P.x0, P.x1, i) - kUnit / 2, y = pk_get(P.y0, P.y1, i) - kUnit / 2;
+        if (px * y - py * x <= 0) return false;
+        // a counter-clockwise step of less than half a turn from the lower to
+        // the upper half-plane passes angle 0
+        const bool up_prev = py > 0 || (py == 0 && px > 0), up = y > 0 || (y == 0 && x > 0);
+        wraps += (!up_prev && up) ? 1 : 0;
+        px = x;
+        py = y;
+    }
+    return wraps == 1;
+}
+
+// Footprint coverage of a simple polygon (vertices x u, in 1/256 output
+// pixel) by crossing number at the sample point shifted by (+e, -e^2): the
+// same set the top-left rule gives for any exact triangulation of it. Each
+// edge toggles, on every sample row it crosses, the samples left of the
+// crossing; the crossing column steps from row to row by an exact rational
+// increment (quotient and remainder), so no division per row.
+__device__ __forceinline__ void crossing_mask(const Packed& P, int u, int mlo, int F, uint32_t* rows, int rstride)
+{
+    const int n = P.n;
+    int bx = pk_get(P.x0, P.x1, n - 1) * u, by = pk_get(P.y0, P.y1, n - 1) * u;
+    for (int i = 0; i < n; i++) {
+        int ax = bx, ay = by;
+        bx = pk_get(P.x0, P.x1, i) * u;
+        by = pk_get(P.y0, P.y1, i) * u;
+        if (ay == by) continue;
+        int lx = ax, ly = ay, hxx = bx, hyy = by;
+        if (ly > hyy) {
+            lx = bx; ly = by; hxx = ax; hyy = ay;
+        }
+        // rows whose sample height py = 256 row + 128 has ly < py <= hyy
+        const int r0 = max(((ly - 128) >> 8) + 1, mlo), r1 = min((hyy - 128) >> 8, mlo + F - 1);
+        if (r0 > r1) continue;
+        const int D = hyy - ly, den = 256 * D;
+        // samples left of the crossing: 256 m + 128 < x_cross  <=>  m < num / den
+        int num = lx * D + (256 * r0 + 128 - ly) * (hxx - lx) - 128 * D;
+        const int step = 256 * (hxx - lx);
+        int q = floor_div(num, den), r = num - q * den;
+        const int sq = floor_div(step, den), sr = step - sq * den;
+        for (int row = r0; row <= r1; row++) {
+            const int k = q + (r > 0 ? 1 : 0) - mlo; // ceil(num / den) - mlo
+            rows[(row - mlo) * rstride] ^= k <= 0 ? 0u : (k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u));
+            q += sq;
+            r += sr;
+            if (r >= den) {
+                r -= den;
+                q++;
+            }
+        }
+    }
+    const uint32_t fmask = F >= 32 ? 0xFFFFFFFFu : ((1u << F) - 1u);
+    for (int row = 0; row < F; row++) rows[row * rstride] &= fmask;
+}
+
+}  // namespace depix

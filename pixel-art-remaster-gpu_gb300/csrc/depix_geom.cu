@@ -608,31 +608,34 @@ __device__ __forceinline__ unsigned spill_bits(int x0, int y0, int x1, int y1)
 template <typename GraphAt, typename TJ>
 __device__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint32_t* rows, int rstride)
 {
-    unsigned node = G(0, 0);
-    int pat = cell_pattern(node, G(-1, 0), G(1, 0));
-    Poly c, sp;
-    hull_from_lut(__ldg(&g_hull_lut[pat]), c);
-    auto nb_hull = [&](int link, Poly& p) {
-        int dx = dir_di(link), dy = dir_dj(link);
-        int np = cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy));
-        hull_from_lut(__ldg(&g_hull_lut[np]), p);
+    const unsigned node = G(0, 0);
+    const uint64_t e = __ldg(&g_hull_lut[cell_pattern(node, G(-1, 0), G(1, 0))]);
+    auto nb_entry = [&](int L) -> uint64_t {
+        const int dx = dir_di(L), dy = dir_dj(L);
+        return __ldg(&g_hull_lut[cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy))]);
     };
-    subdivide_cell(c, node, nb_hull, tj, sp);
-    uint8_t tri[3 * kMaxPoly];
-    bool ok;
-    int nt = ear_clip(sp, tri, ok);
+    Packed sp;
+    subdivide_packed(e, node, nb_entry, tj, sp);
     for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
     const int u = 4 * Gm.s;
-    for (int t = 0; t < nt; t++) {
-        int a = tri[3 * t], b = tri[3 * t + 1], d = tri[3 * t + 2];
-        tri_mask(sp.x[a] * u, sp.y[a] * u, sp.x[b] * u, sp.y[b] * u, sp.x[d] * u, sp.y[d] * u, Gm.mlo, Gm.F, rows,
-                 rstride);
+    if (star_simple(sp)) {
+        // the reference's ear clip would tile the polygon exactly
+        crossing_mask(sp, u, Gm.mlo, Gm.F, rows, rstride);
+    } else {
+        bool ok;
+        const int nt = ear_clip_packed(
+        sp,
+        [&](int ax, int ay, int bx, int by, int cx, int cy) {
+            tri_mask(ax * u, ay * u, bx * u, by * u, cx * u, cy * u, Gm.mlo, Gm.F, rows, rstride);
+        },
+        ok);
+        if (nt == 0) return 0;
     }
-    if (nt == 0) return 0;
     int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
     for (int t = 0; t < sp.n; t++) {
-        mnx = min(mnx, (int)sp.x[t]); mxx = max(mxx, (int)sp.x[t]);
-        mny = min(mny, (int)sp.y[t]); mxy = max(mxy, (int)sp.y[t]);
+        const int x = pk_get(sp.x0, sp.x1, t), y = pk_get(sp.y0, sp.y1, t);
+        mnx = min(mnx, x); mxx = max(mxx, x);
+        mny = min(mny, y); mxy = max(mxy, y);
     }
     return spill_bits(mnx, mny, mxx, mxy);
 }
@@ -645,7 +648,7 @@ int complex_mask_words(int scale) { return mask_geom(scale).F + 1; }
 constexpr int kCxWarpCells = 256;
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(256) k_complex_masks(RasterBatch b)
+__global__ void __launch_bounds__(256, 3) k_complex_masks(RasterBatch b)
 {
     __shared__ int queue[8][64];
     __shared__ uint32_t rows_s[32 * 256];
@@ -661,21 +664,41 @@ __global__ void __launch_bounds__(256) k_complex_masks(RasterBatch b)
 
     auto process = [&](int cell) {
         const int ci = cell % w, cj = cell / w;
+        // the graph bytes any step can read: rows cj-1..cj+1, columns ci-2..ci+2
+        // (own row neighbours, linked neighbours and their row neighbours),
+        // fetched up front as independent loads and kept packed in registers
+        uint32_t gw0 = 0, gw1 = 0, gw2 = 0, gw3 = 0;
+#pragma unroll
+        for (int k = 0; k < 15; k++) {
+            int x = ci + k % 5 - 2, y = cj + k / 5 - 1;
+            uint32_t v = 0;
+            if (x >= 0 && y >= 0 && x < w && y < h) v = __ldg(g + (size_t)y * w + x) & inside_mask(x, y, w, h);
+            v <<= 8 * (k & 3);
+            if (k < 4) gw0 |= v;
+            else if (k < 8) gw1 |= v;
+            else if (k < 12) gw2 |= v;
+            else gw3 |= v;
+        }
         auto G = [&](int dx, int dy) -> unsigned {
-            int x = ci + dx, y = cj + dy;
-            if (x < 0 || y < 0 || x >= w || y >= h) return 0u;
-            return __ldg(g + (size_t)y * w + x) & inside_mask(x, y, w, h);
+            int k = (dy + 1) * 5 + dx + 2;
+            uint32_t wv = k < 4 ? gw0 : (k < 8 ? gw1 : (k < 12 ? gw2 : gw3));
+            return (wv >> (8 * (k & 3))) & 0xFFu;
         };
-        auto tj = [&](int px, int py) -> bool {
+        // the 3x3 pixels of interior cells for the corner tests
+        const bool inner = ci > 0 && ci < w - 1 && cj > 0 && cj < h - 1;
+        uint32_t px[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) px[k] = inner ? load_bgr(img, ws, LAYOUT, ci + k % 3 - 1, cj + k / 3 - 1) : 0u;
+        auto tj = [&](int qx, int qy) -> bool {
             long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
             long long index = (long long)cj * st + (long long)ci * 3;
             if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
-            if (ci == 0 || ci == w - 1 || cj >= h - 1) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
-            auto C = [&](int dx, int dy) { return load_bgr(img, ws, LAYOUT, ci + dx, cj + dy); };
-            if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
-            if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
-            if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
-            if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
+            if (!inner) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, qx, qy);
+            // C(dx, dy) = px[(dy + 1) * 3 + dx + 1]
+            if (qx == 0 && qy == 0) return px[3] != px[0] || px[0] != px[1];
+            if (qx == kUnit && qy == 0) return px[5] != px[2] || px[2] != px[1];
+            if (qx == kUnit && qy == kUnit) return px[7] != px[8] || px[8] != px[5];
+            if (qx == 0 && qy == kUnit) return px[6] != px[7] || px[7] != px[3];
             return false;
         };
         unsigned spill = complex_cell_mask(G, tj, Gm, rows, 256);
