@@ -186,9 +186,8 @@ enum {
     DEPIX_STAGE_GRAPH = 0,      /* similarity graph + trivial removal */
     DEPIX_STAGE_HEURISTICS = 1, /* heuristic crossing resolution */
     DEPIX_STAGE_LABELS = 2,     /* component labels */
-    DEPIX_STAGE_RASTER = 3,     /* cell masks from the pattern tables, block resolution, output */
-    DEPIX_STAGE_SUBDIVIDED = 4, /* subdivided cells: corner cutting, ear clip, coverage masks */
-    DEPIX_STAGE_COUNT = 5
+    DEPIX_STAGE_RASTER = 3,     /* cells, subdivision, coverage masks, block resolution, output */
+    DEPIX_STAGE_COUNT = 4
 };
 /* Turns CUDA-event timing of every stage launch on or off (off by default). */
 depix_status depix_context_set_timing(depix_context* ctx, int enable);

@@ -336,9 +336,6 @@ struct depix_context {
     double ms[DEPIX_STAGE_COUNT] = {};
     long long launches[DEPIX_STAGE_COUNT] = {};
     long long calls[DEPIX_STAGE_COUNT] = {};
-    // subdivided-cell mask scratch (max_pixels * max_frames cells)
-    uint32_t* cmask = nullptr;
-    size_t cmask_words = 0; // words per cell the scratch was sized for
 
     cudaEvent_t take_event()
     {
@@ -378,35 +375,9 @@ struct StageTimer {
     }
 };
 
-// Sizes the subdivided-cell mask scratch for a scale (grows, never shrinks).
-depix_status ensure_cmask(depix_context* c, int scale)
+// Raster of a context call.
+depix_status ctx_raster(depix_context* c, const RasterBatch& rb, int nframes, cudaStream_t s)
 {
-    size_t words = (size_t)complex_mask_words(scale);
-    if (c->cmask && words <= c->cmask_words) return DEPIX_OK;
-    cudaFree(c->cmask);
-    c->cmask = nullptr;
-    c->cmask_words = 0;
-    if (cudaMalloc(&c->cmask, c->max_pixels * (size_t)c->max_frames * words * sizeof(uint32_t)) != cudaSuccess) {
-        cudaGetLastError();
-        t_last_error = "cudaMalloc of the subdivided-cell scratch failed";
-        return DEPIX_ERR_ALLOC;
-    }
-    c->cmask_words = words;
-    return DEPIX_OK;
-}
-
-// Raster of a context call: subdivided cells on their own first (when the
-// scale uses the mask raster), then the tile raster.
-depix_status ctx_raster(depix_context* c, RasterBatch rb, int nframes, size_t cmask_frame_words, size_t cmask_off,
-                        cudaStream_t s)
-{
-    if (rb.subdivide && rb.scale <= kMaxMaskScale) {
-        DEPIX_TRY(ensure_cmask(c, rb.scale));
-        rb.cmask = c->cmask + cmask_off;
-        rb.cmask_stride = cmask_frame_words;
-        StageTimer t(c, DEPIX_STAGE_SUBDIVIDED, 1, s);
-        DEPIX_CK(launch_complex_masks(rb, nframes, s));
-    }
     StageTimer t(c, DEPIX_STAGE_RASTER, 1, s);
     DEPIX_TRY(raster_launch(rb, nframes, s));
     return DEPIX_OK;
@@ -507,7 +478,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         {
             RasterBatch rb{img0, (size_t)is, ctx->graph_b, px, d_out + out_offset[0], (size_t)os, w[0], h[0],
                            4 * w[0], DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
-            DEPIX_TRY(ctx_raster(ctx, rb, n, px * (size_t)complex_mask_words(p->scale), 0, s));
+            DEPIX_TRY(ctx_raster(ctx, rb, n, s));
         }
         return DEPIX_OK;
     }
@@ -532,7 +503,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         {
             RasterBatch rb{img, 0, ctx->graph_b + goff, 0, d_out + out_offset[k], 0, w[k], h[k], 4 * w[k],
                            DEPIX_LAYOUT_RGBA, p->scale, p->subdivide};
-            DEPIX_TRY(ctx_raster(ctx, rb, 1, 0, goff * (size_t)complex_mask_words(p->scale), s));
+            DEPIX_TRY(ctx_raster(ctx, rb, 1, s));
         }
         goff += ctx->max_pixels;
         loff += (size_t)w[k] * h[k];
@@ -575,7 +546,6 @@ depix_status depix_context_destroy(depix_context* c)
     cudaFree(c->stage_in);
     cudaFree(c->stage_out);
     cudaFree(c->stage_labels);
-    cudaFree(c->cmask);
     for (auto& m : c->marks) {
         cudaEventDestroy(m.a);
         cudaEventDestroy(m.b);
@@ -647,7 +617,7 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
     }
     if (d_out) {
         RasterBatch rb{d_img, 0, resolved, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};
-        DEPIX_TRY(ctx_raster(ctx, rb, 1, 0, 0, s));
+        DEPIX_TRY(ctx_raster(ctx, rb, 1, s));
     }
     return DEPIX_OK;
 }

@@ -12,6 +12,14 @@ namespace depix {
 
 __device__ uint64_t g_hull_lut[4096];
 __device__ uint64_t g_tri_lut[4096];
+// Per pattern and hull vertex v: the corner-cutting case of v (bits 0-1:
+// 0 both adjacent edges linked, 1 both border, 2 only the previous edge
+// linked, 3 only the current edge linked) and, for 2 and 3, that edge's link
+// direction (bits 2-4); 5 bits per vertex.
+__device__ uint64_t g_vk_lut[4096];
+// Per pattern and hull vertex v: Q on edge v -> v+1 near v and R on edge
+// v-1 -> v near v (getQ_i(v), getR_i(v-1)), as int8 x, y, x, y in 1/64 cell.
+__device__ __align__(16) uint32_t g_qr_lut[4096 * 8];
 
 // ------------------------------------------------------ pattern tables
 
@@ -137,6 +145,27 @@ __global__ void k_init_tables()
     uint64_t te = 0;
     for (int q = 0; q < 3 * nt; q++) te |= (uint64_t)tri[q] << (3 * q);
     g_tri_lut[pat] = te;
+    // vertex cases and corner-cutting points
+    int links[kMaxHull];
+    for (int v = 0; v < k; v++) links[v] = hull_edge_link(e, k, node, v);
+    uint64_t vk = 0;
+    for (int v = 0; v < kMaxHull; v++) {
+        uint32_t qr = 0;
+        if (v < k) {
+            const int lc = links[v], lp = links[v == 0 ? k - 1 : v - 1];
+            const bool cur = lc >= 0, prev = lp >= 0;
+            const int kind = cur == prev ? (cur ? 0 : 1) : (prev ? 2 : 3);
+            const int L = kind == 2 ? lp : (kind == 3 ? lc : 0);
+            vk |= (uint64_t)(kind | (L << 2)) << (5 * v);
+            int qx, qy, rx, ry;
+            hull_qr(e, k, v, false, qx, qy);
+            hull_qr(e, k, v - 1, true, rx, ry);
+            qr = (uint32_t)(uint8_t)qx | ((uint32_t)(uint8_t)qy << 8) | ((uint32_t)(uint8_t)rx << 16) |
+                 ((uint32_t)(uint8_t)ry << 24);
+        }
+        g_qr_lut[pat * 8 + v] = qr;
+    }
+    g_vk_lut[pat] = vk;
 }
 
 cudaError_t init_tables(cudaStream_t s)
@@ -568,17 +597,18 @@ cudaError_t build_scale_masks(int s, uint32_t* lut, cudaStream_t st)
     return cudaGetLastError();
 }
 
-constexpr int kMTW = 32, kMTH = 16;
-constexpr int kMGW = kMTW + 2, kMGH = kMTH + 2, kMGN = kMGW * kMGH;
-constexpr int kMBW = kMTW + 6, kMBH = kMTH + 6;
-constexpr int kMCW = kMTW + 4, kMCH = kMTH + 4;
+constexpr int kMTW = 32; // tile width in cells; the height is a template parameter
 
-struct MaskShared {
-    uint8_t graph[kMBH][kMBW];
-    uint32_t pix[kMCH][kMCW];
-    uint8_t spill[kMGN];  // bit e: the polygon reaches into the open square of neighbour e
-    uint8_t live[kMGN];   // the cell exists (inside the image)
-    uint16_t list[kMGN];  // subdivided cells of the tile
+template <int TH>
+struct MaskTile {
+    static constexpr int GW = kMTW + 2, GH = TH + 2, GN = GW * GH; // cells with their ring
+    static constexpr int BW = kMTW + 6, BH = TH + 6;               // graph, halo 3
+    static constexpr int CW = kMTW + 4, CH = TH + 4;               // pixels, halo 2
+    uint8_t graph[BH][BW];
+    uint32_t pix[CH][CW];
+    uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
+    uint8_t live[GN];  // the cell exists (inside the image)
+    uint16_t list[GN]; // subdivided cells of the tile
     int count;
 };
 
@@ -600,36 +630,109 @@ __device__ __forceinline__ unsigned spill_bits(int x0, int y0, int x1, int y1)
     return m;
 }
 
+// One corner-cutting round (subdivision, subdivision_functions.cu:564-669)
+// read off the per-pattern tables: each hull vertex's case, its own Q and R
+// points and, on a linked/border transition, the linked neighbour's R (or Q)
+// around the vertex matching this one (getPointIndex falls back to vertex 0).
+// NbPattern(L) is the pattern of the neighbour in direction L; TJ(px, py) the
+// corner test of a vertex between two border edges.
+template <typename NbPattern, typename TJ>
+__device__ __forceinline__ void subdivide_tables(int pat, uint64_t e, NbPattern nb_pattern, TJ tj, Packed& out)
+{
+    const int n = (int)(e & 0xF);
+    const uint64_t vk = __ldg(&g_vk_lut[pat]);
+    const uint4* qrv = reinterpret_cast<const uint4*>(g_qr_lut + pat * 8);
+    const uint4 qa = __ldg(qrv), qb = __ldg(qrv + 1);
+    out.x0 = out.x1 = out.y0 = out.y1 = 0;
+    int m = 0;
+    for (int v = 0; v < n; v++) {
+        const int code = (int)((vk >> (5 * v)) & 31u), kind = code & 3;
+        const int px = hx(e, v), py = hy(e, v);
+        const uint32_t qr = v < 4 ? (v < 2 ? (v == 0 ? qa.x : qa.y) : (v == 2 ? qa.z : qa.w))
+                                  : (v < 6 ? (v == 4 ? qb.x : qb.y) : (v == 6 ? qb.z : qb.w));
+        const int qx = (int8_t)(qr & 0xFF), qy = (int8_t)((qr >> 8) & 0xFF);
+        const int rx = (int8_t)((qr >> 16) & 0xFF), ry = (int8_t)(qr >> 24);
+        if (kind == 0 || (kind == 1 && tj(px, py))) {
+            pk_put(out, m++, px, py);
+        } else if (kind == 1) {
+            pk_put(out, m++, rx, ry);
+            pk_put(out, m++, qx, qy);
+        } else {
+            const int L = code >> 2, ddx = dir_di(L), ddy = dir_dj(L);
+            const int np = nb_pattern(L);
+            const uint64_t ne = __ldg(&g_hull_lut[np]);
+            const int nn = (int)(ne & 0xF);
+            // index of the neighbour hull vertex at this vertex's position
+            // (quarter units in the neighbour's frame), else 0
+            const int tqx = (px - kUnit * ddx) / (kUnit / 4) + 1, tqy = (py - kUnit * ddy) / (kUnit / 4) + 1;
+            int op = 0;
+            if (tqx >= 0 && tqx < 8 && tqy >= 0 && tqy < 8) {
+                const uint64_t key = (uint64_t)(tqx | (tqy << 3)) * 0x041041041041ull;
+                const uint64_t x = ((ne >> 4) & 0xFFFFFFFFFFFFull) ^ key;
+                uint64_t zero = (x - 0x041041041041ull) & ~x & 0x820820820820ull;
+                zero &= (1ull << (6 * nn)) - 1ull; // only the hull's own vertices
+                if (zero) op = (__ffsll((long long)zero) - 1) / 6;
+            }
+            const uint32_t nq = __ldg(&g_qr_lut[np * 8 + op]);
+            int ax, ay;
+            if (kind == 2) { // previous edge linked: the neighbour's R
+                ax = (int8_t)((nq >> 16) & 0xFF);
+                ay = (int8_t)(nq >> 24);
+            } else { // current edge linked: the neighbour's Q
+                ax = (int8_t)(nq & 0xFF);
+                ay = (int8_t)((nq >> 8) & 0xFF);
+            }
+            ax += kUnit * ddx;
+            ay += kUnit * ddy;
+            if (kind == 2) {
+                pk_put(out, m++, (qx + ax) / 2, (qy + ay) / 2);
+                pk_put(out, m++, qx, qy);
+            } else {
+                pk_put(out, m++, rx, ry);
+                pk_put(out, m++, (rx + ax) / 2, (ry + ay) / 2);
+            }
+        }
+    }
+    out.n = m;
+}
+
+// Coverage of a polygon that is not star-shaped around its cell centre: the
+// reference's own ear clip, triangle by triangle. Returns the ear count.
+__device__ __noinline__ int ear_clip_mask(const Packed& P, int u, int mlo, int F, uint32_t* rows, int rstride)
+{
+    bool ok;
+    return ear_clip_packed(
+        P,
+        [&](int ax, int ay, int bx, int by, int cx, int cy) {
+            tri_mask(ax * u, ay * u, bx * u, by * u, cx * u, cy * u, mlo, F, rows, rstride);
+        },
+        ok);
+}
+
 // Footprint mask rows (F words at rows[r * rstride]) and spill bits of one
-// subdivided cell: corner cutting against the linked neighbours' hulls, the
-// reference's ear clip, then the triangles' coverage. G(dx, dy) is the graph
-// byte of the cell at that offset (0 outside the image, bits toward outside
-// cleared); TJ(px, py) the corner test.
+// subdivided cell. G(dx, dy) is the graph byte of the cell at that offset
+// (0 outside the image, bits toward outside cleared); TJ(px, py) the corner
+// test.
 template <typename GraphAt, typename TJ>
-__device__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint32_t* rows, int rstride)
+__device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint32_t* rows,
+                                                      int rstride)
 {
     const unsigned node = G(0, 0);
-    const uint64_t e = __ldg(&g_hull_lut[cell_pattern(node, G(-1, 0), G(1, 0))]);
-    auto nb_entry = [&](int L) -> uint64_t {
+    const int pat = cell_pattern(node, G(-1, 0), G(1, 0));
+    const uint64_t e = __ldg(&g_hull_lut[pat]);
+    auto nb_pattern = [&](int L) -> int {
         const int dx = dir_di(L), dy = dir_dj(L);
-        return __ldg(&g_hull_lut[cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy))]);
+        return cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy));
     };
     Packed sp;
-    subdivide_packed(e, node, nb_entry, tj, sp);
+    subdivide_tables(pat, e, nb_pattern, tj, sp);
     for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
     const int u = 4 * Gm.s;
     if (star_simple(sp)) {
         // the reference's ear clip would tile the polygon exactly
         crossing_mask(sp, u, Gm.mlo, Gm.F, rows, rstride);
-    } else {
-        bool ok;
-        const int nt = ear_clip_packed(
-        sp,
-        [&](int ax, int ay, int bx, int by, int cx, int cy) {
-            tri_mask(ax * u, ay * u, bx * u, by * u, cx * u, cy * u, Gm.mlo, Gm.F, rows, rstride);
-        },
-        ok);
-        if (nt == 0) return 0;
+    } else if (ear_clip_mask(sp, u, Gm.mlo, Gm.F, rows, rstride) == 0) {
+        return 0;
     }
     int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
     for (int t = 0; t < sp.n; t++) {
@@ -640,131 +743,34 @@ __device__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint
     return spill_bits(mnx, mny, mxx, mxy);
 }
 
-int complex_mask_words(int scale) { return mask_geom(scale).F + 1; }
-
-// Subdivided-cell masks for whole frames. Each warp scans 256 consecutive
-// cells 32 at a time, queues the subdivided ones with a ballot and works them
-// off 32 at a time, so every lane has a cell and nothing waits on the block.
-constexpr int kCxWarpCells = 256;
-
-template <int LAYOUT>
-__global__ void __launch_bounds__(256, 3) k_complex_masks(RasterBatch b)
+template <int LAYOUT, int S, int TH>
+__device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
+                                 uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
+                                 int y0)
 {
-    __shared__ int queue[8][64];
-    __shared__ uint32_t rows_s[32 * 256];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t z = blockIdx.z;
-    const uint8_t* img = b.img + b.img_stride * z;
-    const uint8_t* g = b.graph + b.graph_stride * z;
-    uint32_t* cm = b.cmask + b.cmask_stride * z;
-    const int w = b.w, h = b.h, ws = b.ws, n = w * h;
-    const MaskGeom Gm = mask_geom(b.scale);
-    const int words = Gm.F + 1;
-    uint32_t* rows = rows_s + threadIdx.x;
-
-    auto process = [&](int cell) {
-        const int ci = cell % w, cj = cell / w;
-        // the graph bytes any step can read: rows cj-1..cj+1, columns ci-2..ci+2
-        // (own row neighbours, linked neighbours and their row neighbours),
-        // fetched up front as independent loads and kept packed in registers
-        uint32_t gw0 = 0, gw1 = 0, gw2 = 0, gw3 = 0;
-#pragma unroll
-        for (int k = 0; k < 15; k++) {
-            int x = ci + k % 5 - 2, y = cj + k / 5 - 1;
-            uint32_t v = 0;
-            if (x >= 0 && y >= 0 && x < w && y < h) v = __ldg(g + (size_t)y * w + x) & inside_mask(x, y, w, h);
-            v <<= 8 * (k & 3);
-            if (k < 4) gw0 |= v;
-            else if (k < 8) gw1 |= v;
-            else if (k < 12) gw2 |= v;
-            else gw3 |= v;
-        }
-        auto G = [&](int dx, int dy) -> unsigned {
-            int k = (dy + 1) * 5 + dx + 2;
-            uint32_t wv = k < 4 ? gw0 : (k < 8 ? gw1 : (k < 12 ? gw2 : gw3));
-            return (wv >> (8 * (k & 3))) & 0xFFu;
-        };
-        // the 3x3 pixels of interior cells for the corner tests
-        const bool inner = ci > 0 && ci < w - 1 && cj > 0 && cj < h - 1;
-        uint32_t px[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) px[k] = inner ? load_bgr(img, ws, LAYOUT, ci + k % 3 - 1, cj + k / 3 - 1) : 0u;
-        auto tj = [&](int qx, int qy) -> bool {
-            long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
-            long long index = (long long)cj * st + (long long)ci * 3;
-            if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
-            if (!inner) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, qx, qy);
-            // C(dx, dy) = px[(dy + 1) * 3 + dx + 1]
-            if (qx == 0 && qy == 0) return px[3] != px[0] || px[0] != px[1];
-            if (qx == kUnit && qy == 0) return px[5] != px[2] || px[2] != px[1];
-            if (qx == kUnit && qy == kUnit) return px[7] != px[8] || px[8] != px[5];
-            if (qx == 0 && qy == kUnit) return px[6] != px[7] || px[7] != px[3];
-            return false;
-        };
-        unsigned spill = complex_cell_mask(G, tj, Gm, rows, 256);
-        uint32_t* o = cm + (size_t)cell * words;
-        for (int r = 0; r < Gm.F; r++) o[r] = rows[r * 256];
-        o[Gm.F] = spill;
-    };
-
-    const int base = blockIdx.x * (8 * kCxWarpCells) + warp * kCxWarpCells;
-    int qn = 0;
-    for (int r = 0; r < kCxWarpCells / 32; r++) {
-        int cell = base + r * 32 + lane;
-        bool cx = cell < n && g[cell] != 90;
-        unsigned bal = __ballot_sync(0xFFFFFFFFu, cx);
-        if (cx) queue[warp][qn + __popc(bal & ((1u << lane) - 1u))] = cell;
-        qn += __popc(bal);
-        __syncwarp();
-        if (qn >= 32) {
-            process(queue[warp][lane]);
-            __syncwarp();
-            if (lane < qn - 32) queue[warp][lane] = queue[warp][lane + 32];
-            qn -= 32;
-            __syncwarp();
-        }
-    }
-    if (lane < qn) process(queue[warp][lane]);
-}
-
-cudaError_t launch_complex_masks(const RasterBatch& b, int nframes, cudaStream_t s)
-{
-    int n = b.w * b.h;
-    dim3 grid((n + 8 * kCxWarpCells - 1) / (8 * kCxWarpCells), 1, nframes);
-    if (b.layout == DEPIX_LAYOUT_RGBA)
-        k_complex_masks<DEPIX_LAYOUT_RGBA><<<grid, 256, 0, s>>>(b);
-    else
-        k_complex_masks<DEPIX_LAYOUT_BGR><<<grid, 256, 0, s>>>(b);
-    return cudaGetLastError();
-}
-
-template <int LAYOUT, int S>
-__device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
-                                 uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut,
-                                 const uint32_t* cmask, int x0, int y0)
-{
+    using T = MaskTile<TH>;
     const int s = S > 0 ? S : scale;
     const MaskGeom G = mask_geom(s);
     const int F = G.F;
     // ---- phase A
     if (threadIdx.x == 0) M.count = 0;
-    for (int k = threadIdx.x; k < kMBW * kMBH; k += blockDim.x) {
-        int gx = x0 - 3 + k % kMBW, gy = y0 - 3 + k / kMBW;
+    for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
+        int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
         unsigned v = 0;
         if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = __ldg(g + (size_t)gy * w + gx) & inside_mask(gx, gy, w, h);
-        M.graph[k / kMBW][k % kMBW] = (uint8_t)v;
+        M.graph[k / T::BW][k % T::BW] = (uint8_t)v;
     }
-    for (int k = threadIdx.x; k < kMCW * kMCH; k += blockDim.x) {
-        int gx = x0 - 2 + k % kMCW, gy = y0 - 2 + k / kMCW;
+    for (int k = threadIdx.x; k < T::CW * T::CH; k += blockDim.x) {
+        int gx = x0 - 2 + k % T::CW, gy = y0 - 2 + k / T::CW;
         uint32_t v = 0;
         if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = load_bgr(img, ws, LAYOUT, gx, gy);
-        M.pix[k / kMCW][k % kMCW] = v;
+        M.pix[k / T::CW][k % T::CW] = v;
     }
     __syncthreads();
 
     // ---- phase B: plain cells from the table, subdivided cells to the list
-    for (int k = threadIdx.x; k < kMGN; k += blockDim.x) {
-        int lx = k % kMGW, ly = k / kMGW;
+    for (int k = threadIdx.x; k < T::GN; k += blockDim.x) {
+        int lx = k % T::GW, ly = k / T::GW;
         int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
         uint32_t* rows = masks + (size_t)k * F;
         bool live = ci >= 0 && cj >= 0 && ci < w && cj < h;
@@ -777,14 +783,8 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
         const int bx = lx + 2, by = ly + 2;
         unsigned node = M.graph[by][bx];
         if (subdivide && node != 90) {
-            if (cmask) {
-                const uint32_t* src = cmask + ((size_t)cj * w + ci) * (F + 1);
-                for (int r = 0; r < F; r++) rows[r] = __ldg(src + r);
-                M.spill[k] = (uint8_t)__ldg(src + F);
-            } else {
-                int slot = atomicAdd(&M.count, 1);
-                M.list[slot] = (uint16_t)k;
-            }
+            int slot = atomicAdd(&M.count, 1);
+            M.list[slot] = (uint16_t)k;
             continue;
         }
         int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
@@ -794,22 +794,22 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
             int q = r - dr;
             rows[r] = (q >= 0 && q < G.HF) ? (__ldg(src + q) << dr) : 0u;
         }
-        Poly c;
-        hull_from_lut(__ldg(&g_hull_lut[pat]), c);
+        const uint64_t e = __ldg(&g_hull_lut[pat]);
+        const int n = (int)(e & 0xF);
         int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
-        for (int t = 0; t < c.n; t++) {
-            mnx = min(mnx, c.x[t]); mxx = max(mxx, c.x[t]);
-            mny = min(mny, c.y[t]); mxy = max(mxy, c.y[t]);
+        for (int t = 0; t < n; t++) {
+            mnx = min(mnx, hx(e, t)); mxx = max(mxx, hx(e, t));
+            mny = min(mny, hy(e, t)); mxy = max(mxy, hy(e, t));
         }
         M.spill[k] = (uint8_t)spill_bits(mnx, mny, mxx, mxy);
     }
     __syncthreads();
 
-    // ---- phase B2: subdivided cells, one per thread (when not precomputed)
+    // ---- phase B2: subdivided cells, one per thread
     const int nlist = M.count;
     for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
         int k = M.list[q];
-        int lx = k % kMGW, ly = k / kMGW;
+        int lx = k % T::GW, ly = k / T::GW;
         int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
         const int bx = lx + 2, by = ly + 2;
         auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx]; };
@@ -834,15 +834,15 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
     const int ow = w * s;
     const bool vec = ((S == 4 || S == 8) && (ow % 4) == 0 && ((reinterpret_cast<uintptr_t>(out) & 15) == 0));
     const uint32_t blockbits = (s >= 32) ? 0xFFFFFFFFu : ((1u << s) - 1u);
-    for (int q = threadIdx.x; q < kMTW * kMTH; q += blockDim.x) {
+    for (int q = threadIdx.x; q < kMTW * TH; q += blockDim.x) {
         int tx = q % kMTW, ty = q / kMTW;
         int ci = x0 + tx, cj = y0 + ty;
         if (ci >= w || cj >= h) continue;
-        const int k0 = (ty + 1) * kMGW + (tx + 1);
+        const int k0 = (ty + 1) * T::GW + (tx + 1);
         unsigned intr = 0;
 #pragma unroll
         for (int e = 0; e < 8; e++) {
-            int kn = k0 + dir_dj(e) * kMGW + dir_di(e);
+            int kn = k0 + dir_dj(e) * T::GW + dir_di(e);
             intr |= (unsigned)bitof(M.spill[kn], 7 - e);
         }
         const uint32_t* own = masks + (size_t)k0 * F;
@@ -875,7 +875,7 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
                     take[qq] = 0;
                     col_of[qq] = 0;
                     if (rr < 0 || rr >= F) continue;
-                    int kn = k0 + dj * kMGW + di;
+                    int kn = k0 + dj * T::GW + di;
                     if (!M.live[kn]) continue;
                     uint64_t wbits = masks[(size_t)kn * F + rr];
                     int sh = s * di + G.mlo; // block column c = footprint column + sh
@@ -909,44 +909,48 @@ __device__ void mask_raster_tile(MaskShared& M, uint32_t* masks, const uint8_t* 
     }
 }
 
-template <int LAYOUT, int S>
+template <int LAYOUT, int S, int TH>
 __global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32_t* lut)
 {
-    __shared__ MaskShared M;
+    __shared__ MaskTile<TH> M;
     extern __shared__ uint32_t masks[];
     size_t z = blockIdx.z;
-    mask_raster_tile<LAYOUT, S>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
-                                b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut,
-                                b.cmask ? b.cmask + b.cmask_stride * z : nullptr, blockIdx.x * kMTW, blockIdx.y * kMTH);
+    mask_raster_tile<LAYOUT, S, TH>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
+                                    b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut,
+                                    blockIdx.x * kMTW, blockIdx.y * TH);
 }
 
-template <int LAYOUT, int S>
+template <int LAYOUT, int S, int TH>
 static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
 {
     MaskGeom g = mask_geom(b.scale);
-    size_t smem = (size_t)kMGN * g.F * sizeof(uint32_t);
-    if (smem + sizeof(MaskShared) > 48 * 1024) {
+    size_t smem = (size_t)MaskTile<TH>::GN * g.F * sizeof(uint32_t);
+    if (smem + sizeof(MaskTile<TH>) > 48 * 1024) {
         // opt in to more than 48 KB of shared memory in total (a per-device
         // function attribute; setting it again is harmless)
-        cudaError_t e = cudaFuncSetAttribute(k_mask_raster<LAYOUT, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_mask_raster<LAYOUT, S, TH>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    dim3 grid((b.w + kMTW - 1) / kMTW, (b.h + kMTH - 1) / kMTH, nframes);
-    k_mask_raster<LAYOUT, S><<<grid, 256, smem, s>>>(b, lut);
+    dim3 grid((b.w + kMTW - 1) / kMTW, (b.h + TH - 1) / TH, nframes);
+    k_mask_raster<LAYOUT, S, TH><<<grid, 256, smem, s>>>(b, lut);
     return cudaGetLastError();
 }
 
+// 32x32-cell tiles up to scale 4 (more subdivided cells per block to share
+// the work), 32x16 above (the footprint masks grow with the scale)
 cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
 {
     if (b.layout == DEPIX_LAYOUT_RGBA) {
-        if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4>(b, nframes, lut, s);
-        if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 8>(b, nframes, lut, s);
-        return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0>(b, nframes, lut, s);
+        if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4, 32>(b, nframes, lut, s);
+        if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 8, 16>(b, nframes, lut, s);
+        if (b.scale < 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0, 32>(b, nframes, lut, s);
+        return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0, 16>(b, nframes, lut, s);
     }
-    if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4>(b, nframes, lut, s);
-    if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 8>(b, nframes, lut, s);
-    return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0>(b, nframes, lut, s);
+    if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4, 32>(b, nframes, lut, s);
+    if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 8, 16>(b, nframes, lut, s);
+    if (b.scale < 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 32>(b, nframes, lut, s);
+    return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 16>(b, nframes, lut, s);
 }
 
 size_t scale_mask_words(int s) { return (size_t)4096 * mask_geom(s).HF; }

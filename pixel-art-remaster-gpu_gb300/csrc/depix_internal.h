@@ -47,11 +47,6 @@ struct RasterBatch {
     int w, h, ws, layout;
     int scale;
     int subdivide;
-    // masks of the subdivided cells, precomputed by launch_complex_masks:
-    // (F + 1) words per pixel (F footprint rows, then the spill bits), frames
-    // cmask_stride words apart; NULL when the raster computes them itself
-    uint32_t* cmask;
-    size_t cmask_stride;
 };
 
 // One frame of a variable-size batch (device array entry).
@@ -90,8 +85,6 @@ constexpr int kMaxMaskScale = 12;
 size_t scale_mask_words(int scale);
 cudaError_t build_scale_masks(int scale, uint32_t* lut, cudaStream_t s);
 cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s);
-// words per pixel of the subdivided-cell mask scratch at a scale
-int complex_mask_words(int scale);
-cudaError_t launch_complex_masks(const RasterBatch& b, int nframes, cudaStream_t s);
+
 
 }  // namespace depix

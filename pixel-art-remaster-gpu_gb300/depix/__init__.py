@@ -209,13 +209,13 @@ class Context:
     def set_timing(self, on=True):
         _check(lib().depix_context_set_timing(self.handle, int(bool(on))), "depix_context_set_timing")
 
-    STAGES = ("graph", "heuristics", "labels", "raster", "subdivided")
+    STAGES = ("graph", "heuristics", "labels", "raster")
 
     def stage_times(self):
         """{stage: (ms, launches, calls)} accumulated since the last call."""
-        ms = (ctypes.c_double * 5)()
-        la = (ctypes.c_longlong * 5)()
-        ca = (ctypes.c_longlong * 5)()
+        ms = (ctypes.c_double * 4)()
+        la = (ctypes.c_longlong * 4)()
+        ca = (ctypes.c_longlong * 4)()
         _check(lib().depix_context_stage_times(self.handle, ms, la, ca), "depix_context_stage_times")
         return {name: (ms[k], la[k], ca[k]) for k, name in enumerate(self.STAGES)}
 
