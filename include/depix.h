@@ -143,6 +143,27 @@ depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, 
  * in quarter cells) and its ear clip (3 bits per corner index). Synchronous. */
 depix_status depix_pattern_tables(uint64_t* h_hull, uint64_t* h_tri);
 
+/* Heuristic crossing resolution IN PLACE, allocating nothing. No counterpart
+ * in the reference: it is depix_resolve_heuristics with the snapshot the
+ * heuristics read (the reference's graph_aux copy, kernel.cu:415) kept in a
+ * fixed device array inside the library instead of a caller buffer, for
+ * callers that cannot allocate device memory: real-time or embedded hosts
+ * that forbid allocation after start-up, plugins running under a host
+ * application that owns the device memory pool, code that must not call
+ * cudaMalloc while other work is in flight.
+ *  - d_graph (w*h bytes) holds the graph after trivial removal on entry and
+ *    the resolved graph on return;
+ *  - w*h must not exceed DEPIX_STATIC_MAX_PIXELS (4 MiB of snapshot, e.g.
+ *    2048x2048); larger frames return DEPIX_ERR_TOO_LARGE;
+ *  - every device that loads the library holds the 4 MiB array until the
+ *    process exits;
+ *  - the first call on a device looks up the array's device address (no
+ *    allocation); make that first call before capturing any stream;
+ *  - all calls share the one array: calls whose work overlaps on the GPU
+ *    (different streams, no ordering between them) race on it. */
+#define DEPIX_STATIC_MAX_PIXELS 4194304
+depix_status depix_resolve_heuristics_static(uint8_t* d_graph, int w, int h, depix_stream s);
+
 /* ---------------------------------------------------------------------
  * Frame path with a context that owns its scratch (no allocation per call).
  * --------------------------------------------------------------------- */

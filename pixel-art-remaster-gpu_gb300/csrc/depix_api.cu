@@ -15,6 +15,12 @@ namespace {
 
 thread_local std::string t_last_error;
 
+}  // namespace
+
+void depix::set_last_error(const std::string& msg) { t_last_error = msg; }
+
+namespace {
+
 depix_status cuda_fail(cudaError_t e, const char* where)
 {
     t_last_error = std::string(where) + ": " + cudaGetErrorString(e);

@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "depix_device.cuh"
@@ -60,6 +61,9 @@ struct BatchFrame {
     int tile_base_rast;  // first raster-stage tile index
     int pad;
 };
+
+// text returned by depix_last_error() on this thread
+void set_last_error(const std::string& msg);
 
 // graph stage
 cudaError_t launch_graph(const FrameBatch& b, int nframes, uint32_t thr, bool fuse_trivial, cudaStream_t s);
