@@ -20,6 +20,9 @@ __device__ uint64_t g_vk_lut[4096];
 // Per pattern and hull vertex v: Q on edge v -> v+1 near v and R on edge
 // v-1 -> v near v (getQ_i(v), getR_i(v-1)), as int8 x, y, x, y in 1/64 cell.
 __device__ __align__(16) uint32_t g_qr_lut[4096 * 8];
+// Per pattern: bit e set when the hull reaches into the open square of
+// neighbour e (hull bounding box test).
+__device__ uint8_t g_spill_lut[4096];
 
 // ------------------------------------------------------ pattern tables
 
@@ -166,6 +169,17 @@ __global__ void k_init_tables()
         g_qr_lut[pat * 8 + v] = qr;
     }
     g_vk_lut[pat] = vk;
+    int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
+    for (int t = 0; t < k; t++) {
+        mnx = min(mnx, hx(e, t)); mxx = max(mxx, hx(e, t));
+        mny = min(mny, hy(e, t)); mxy = max(mxy, hy(e, t));
+    }
+    unsigned sp = 0;
+    for (int d = 0; d < 8; d++) {
+        int sx = kUnit * dir_di(d), sy = kUnit * dir_dj(d);
+        if (mxx > sx && mnx < sx + kUnit && mxy > sy && mny < sy + kUnit) sp |= 1u << d;
+    }
+    g_spill_lut[pat] = (uint8_t)sp;
 }
 
 cudaError_t init_tables(cudaStream_t s)
@@ -794,14 +808,7 @@ __device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t
             int q = r - dr;
             rows[r] = (q >= 0 && q < G.HF) ? (__ldg(src + q) << dr) : 0u;
         }
-        const uint64_t e = __ldg(&g_hull_lut[pat]);
-        const int n = (int)(e & 0xF);
-        int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
-        for (int t = 0; t < n; t++) {
-            mnx = min(mnx, hx(e, t)); mxx = max(mxx, hx(e, t));
-            mny = min(mny, hy(e, t)); mxy = max(mxy, hy(e, t));
-        }
-        M.spill[k] = (uint8_t)spill_bits(mnx, mny, mxx, mxy);
+        M.spill[k] = __ldg(&g_spill_lut[pat]);
     }
     __syncthreads();
 
@@ -863,47 +870,48 @@ __device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t
             continue;
         }
         for (int r = 0; r < s; r++) {
-            uint32_t colour[S > 0 ? S : 16];
-            const int ncol = s;
+            // per candidate (priority order q = 0..8: rows above first, then
+            // right to left) the samples of this row it covers and no
+            // earlier candidate does; candidates are one cell apart so the
+            // nine masks are disjoint and each sample has at most one owner
             uint32_t claimed = 0;
-            uint32_t col_of[9];
             uint32_t take[9];
             int qq = 0;
+#pragma unroll
             for (int dj = 1; dj >= -1; dj--) {
-                int rr = r - s * dj - G.mlo;
+                const int rr = r - s * dj - G.mlo;
+#pragma unroll
                 for (int di = 1; di >= -1; di--, qq++) {
                     take[qq] = 0;
-                    col_of[qq] = 0;
                     if (rr < 0 || rr >= F) continue;
-                    int kn = k0 + dj * T::GW + di;
+                    const int kn = k0 + dj * T::GW + di;
                     if (!M.live[kn]) continue;
-                    uint64_t wbits = masks[(size_t)kn * F + rr];
-                    int sh = s * di + G.mlo; // block column c = footprint column + sh
-                    uint32_t bits = (uint32_t)((sh >= 0 ? (wbits << sh) : (wbits >> (-sh))) & blockbits);
-                    uint32_t t = bits & ~claimed;
-                    claimed |= t;
-                    take[qq] = t;
-                    col_of[qq] = rgba_of(M.pix[ty + 2 + dj][tx + 2 + di]);
+                    const uint64_t wbits = masks[(size_t)kn * F + rr];
+                    const int sh = s * di + G.mlo; // block column c = footprint column + sh
+                    const uint32_t bits =
+                        (uint32_t)((sh >= 0 ? (wbits << sh) : (wbits >> (-sh))) & blockbits) & ~claimed;
+                    claimed |= bits;
+                    take[qq] = bits;
                 }
             }
-#pragma unroll
-            for (int c = 0; c < (S > 0 ? S : 16); c++) {
-                if (c >= ncol) break;
-                uint32_t v = 0xFF000000u;
-#pragma unroll
-                for (int z = 0; z < 9; z++)
-                    if ((take[z] >> c) & 1u) v = col_of[z];
-                colour[c] = v;
-            }
             uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
+            auto owner_colour = [&](int c) -> uint32_t {
+                if (!((claimed >> c) & 1u)) return 0xFF000000u;
+                int z = 0;
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                    if ((take[q] >> c) & 1u) z = q;
+                // candidate z is the cell (di, dj) = (1 - z % 3, 1 - z / 3)
+                return rgba_of(M.pix[ty + 2 + 1 - z / 3][tx + 2 + 1 - z % 3]);
+            };
             if (vec) {
 #pragma unroll
                 for (int c4 = 0; c4 < (S > 0 ? S : 16); c4 += 4)
-                    if (c4 < ncol)
-                        __stcs(reinterpret_cast<uint4*>(o + c4),
-                               make_uint4(colour[c4], colour[c4 + 1], colour[c4 + 2], colour[c4 + 3]));
+                    if (c4 < s)
+                        __stcs(reinterpret_cast<uint4*>(o + c4), make_uint4(owner_colour(c4), owner_colour(c4 + 1),
+                                                                            owner_colour(c4 + 2), owner_colour(c4 + 3)));
             } else {
-                for (int c = 0; c < ncol; c++) o[c] = colour[c];
+                for (int c = 0; c < s; c++) o[c] = owner_colour(c);
             }
         }
     }

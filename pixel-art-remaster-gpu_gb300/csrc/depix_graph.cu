@@ -342,16 +342,27 @@ __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, 
 }
 
 // unions across tile borders: every set bit whose neighbour lies in another
-// tile (each symmetric pair is seen from both ends; uniting twice is harmless)
+// tile (each symmetric pair is seen from both ends; uniting twice is
+// harmless). One thread per border pixel of a tile (4 * 32 - 4 of them).
+constexpr int kLBorder = 4 * kLT - 4;
+
 __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= w * h) return;
-    int i = k % w, j = k / w;
-    int ti = i % kLT, tj = j % kLT;
-    if (ti != 0 && ti != kLT - 1 && tj != 0 && tj != kLT - 1) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tiles_x = (w + kLT - 1) / kLT, tiles_y = (h + kLT - 1) / kLT;
+    const int tile = t / kLBorder, q = t % kLBorder;
+    if (tile >= tiles_x * tiles_y) return;
+    // border position q: bottom row, top row, then left and right columns
+    int lx, ly;
+    if (q < kLT) { lx = q; ly = 0; }
+    else if (q < 2 * kLT) { lx = q - kLT; ly = kLT - 1; }
+    else if (q < 3 * kLT - 2) { lx = 0; ly = q - 2 * kLT + 1; }
+    else { lx = kLT - 1; ly = q - (3 * kLT - 2) + 1; }
+    const int i = (tile % tiles_x) * kLT + lx, j = (tile / tiles_x) * kLT + ly;
+    if (i >= w || j >= h) return;
     g += frame_stride * blockIdx.z;
     L += frame_stride * blockIdx.z;
+    const int k = j * w + i;
     unsigned node = g[k];
 #pragma unroll
     for (int e = 0; e < 8; e++) {
@@ -417,8 +428,9 @@ cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int n
     int n = w * h;
     dim3 tiles((w + kLT - 1) / kLT, (h + kLT - 1) / kLT, nframes);
     k_cc_local<<<tiles, 256, 0, s>>>(g, labels, w, h, frame_stride);
+    const int borders = tiles.x * tiles.y * kLBorder;
+    k_cc_merge<<<dim3((borders + 127) / 128, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
     dim3 grid((n + 255) / 256, 1, nframes);
-    k_cc_merge<<<grid, 256, 0, s>>>(g, labels, w, h, frame_stride);
     k_cc_flatten<<<grid, 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }
