@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=0, help="default: max(3, steps // 20)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU-baseline sample (default 4 x cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--sprites", type=int, default=4096, help="sprites in the uneven-batch leg")
+    ap.add_argument("--no-sprites", action="store_true")
     return ap.parse_args()
 
 
@@ -288,6 +290,8 @@ def run_ours(args, rank, world, local_rank):
              "p99_ms_per_frame": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4), "frames": pf}
     ctx1.close()
 
+    sprites = None if args.no_sprites else run_sprites(args, dev, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cores = cpu_setup()
@@ -303,8 +307,91 @@ def run_ours(args, rank, world, local_rank):
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
-                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites}
         print(json.dumps(line))
+
+
+def run_sprites(args, dev, stream):
+    """Uneven batch: 4096 sprites with sides ~ U[8, 64] (30 % transparent
+    backgrounds), x4, with labels, in one depix_batch call per step (the
+    persistent tile-queue path, replayed as a graph, launch shape tuned on
+    the first call), against one plain per-frame call per sprite."""
+    import numpy as np
+    import torch
+    import depix
+    from depix import synth
+
+    imgs = synth.sprites(args.sprites, seed=0)
+    ws, hs = [i.shape[1] for i in imgs], [i.shape[0] for i in imgs]
+    in_off, out_off, oi, oo = [], [], 0, 0
+    for w, h in zip(ws, hs):
+        in_off.append(oi)
+        out_off.append(oo)
+        oi += (w * h * 4 + 15) // 16 * 16
+        oo += (w * h * 64 + 15) // 16 * 16
+    buf = np.zeros(oi, np.uint8)
+    for k, img in enumerate(imgs):
+        buf[in_off[k]:in_off[k] + img.size] = img.reshape(-1)
+    npx = sum(w * h for w, h in zip(ws, hs))
+    d_in = torch.from_numpy(buf).to(dev)
+    d_out = torch.empty(oo, dtype=torch.uint8, device=dev)
+    d_lab = torch.empty(npx, dtype=torch.int32, device=dev)
+    p = depix.params(48, 7, 6, True, SCALE)
+    ctx = depix.Context(64 * 64, len(imgs))
+
+    def step():
+        ctx.batch(ws, hs, in_off, out_off, d_in, p, d_out, d_lab, stream=stream)
+
+    t0 = time.perf_counter()
+    step()  # tunes the launch shape for this size bucket
+    torch.cuda.synchronize()
+    tune_s = time.perf_counter() - t0
+    for _ in range(3):
+        step()
+    steps = max(10, args.steps // 3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ctx.set_timing(True)
+    for _ in range(5):
+        step()
+    torch.cuda.synchronize()
+    ctx.set_timing(False)
+    st = ctx.stage_times()
+    gran, tw, th = ctx.launch_shape()
+
+    # plain: one depix_frame call (one launch per stage) per sprite
+    ctx1 = depix.Context(64 * 64, 1)
+
+    def plain():
+        for k in range(len(imgs)):
+            ctx1.frame(d_in[in_off[k]:], ws[k], hs[k], 4 * ws[k], depix.LAYOUT_RGBA, p, d_out[out_off[k]:], None,
+                       d_lab, stream=stream)
+
+    plain()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    t0 = time.perf_counter()
+    plain()
+    b.record(stream)
+    torch.cuda.synchronize()
+    plain_wall = time.perf_counter() - t0
+    plain_ms = a.elapsed_time(b)
+    ctx1.close()
+    ctx.close()
+    n = len(imgs)
+    return {"workload": f"{n} sprites, sides ~ U[8,64] (seeded generator), {npx} px in, x4 RGBA8 out, labels",
+            "frames_per_s": round(n / (ms / 1e3), 1), "ms_per_batch": round(ms, 4),
+            "out_mpix_per_s": round(npx * SCALE * SCALE / (ms / 1e3) / 1e6, 1), "steps": steps,
+            "stage_ms_per_batch": {k: round(v[0] / max(v[2], 1), 4) for k, v in st.items()},
+            "launch_shape": {"gran": list(gran), "raster_tile": [tw, th]}, "first_call_s": round(tune_s, 3),
+            "plain_frames_per_s": round(n / (plain_ms / 1e3), 1), "plain_host_wall_s": round(plain_wall, 3)}
 
 
 # ---------------------------------------------------------- reference arm

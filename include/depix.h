@@ -187,7 +187,9 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
  * bytes and must be multiples of 16. With d_labels set, frame k's component
  * labels go to d_labels + (w[0]*h[0] + ... + w[k-1]*h[k-1]). Host arrays w,
  * h, in_offset, out_offset have n entries. Frames of one size at a constant
- * stride go through one launch per stage for the whole batch. */
+ * stride go through one launch per stage for the whole batch; other batches
+ * (scale up to 12, stream not capturing) through persistent kernels that pull
+ * tiles of all frames from one queue per stage, replayed as a CUDA graph. */
 depix_status depix_batch(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
                          const uint64_t* out_offset, const uint8_t* d_img, const depix_params* p, uint8_t* d_out,
                          int32_t* d_labels, depix_stream s);
@@ -201,6 +203,16 @@ depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int
                               const uint64_t* out_offset, const uint8_t* h_img, size_t in_bytes,
                               const depix_params* p, uint8_t* h_out, size_t out_bytes, int32_t* h_labels,
                               depix_stream s);
+
+/* Launch shape of the queue path (uneven batches): tiles pulled per queue
+ * step, 1, 2, 4 or 8 (0: tuned, the default), and the raster tile in cells,
+ * 32x32, 32x16 or 16x16. Tuning runs on the first batch of each bucket of
+ * frame count and mean frame size (powers of two), scale and label choice, by
+ * timing the candidate shapes on that batch (it synchronises the stream). */
+depix_status depix_context_set_launch_shape(depix_context* ctx, int gran, int tile_w, int tile_h);
+/* The shape the last queue-path batch ran with: gran[4] per stage (graph,
+ * heuristics, labels, raster) and the raster tile; any pointer may be NULL. */
+depix_status depix_context_launch_shape(depix_context* ctx, int* gran, int* tile_w, int* tile_h);
 
 /* Per-stage device timing of a context's frame and batch calls. */
 enum {

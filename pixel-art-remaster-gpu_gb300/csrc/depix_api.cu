@@ -342,6 +342,10 @@ struct depix_context {
     double ms[DEPIX_STAGE_COUNT] = {};
     long long launches[DEPIX_STAGE_COUNT] = {};
     long long calls[DEPIX_STAGE_COUNT] = {};
+    // uneven batches (created on the first one)
+    QueueRunner* queue = nullptr;
+    bool shape_forced = false;
+    QueueShape shape{};
 
     cudaEvent_t take_event()
     {
@@ -488,7 +492,31 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         }
         return DEPIX_OK;
     }
-    // uneven frames: one launch per stage and frame
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    DEPIX_CK(cudaStreamIsCapturing(s, &cs));
+    if (p->scale <= kMaxMaskScale && cs == cudaStreamCaptureStatusNone) {
+        // uneven frames: persistent kernels over one tile queue per stage
+        if (!ctx->queue) DEPIX_TRY(queue_runner_create(ctx->max_frames, &ctx->queue));
+        queue_force_shape(ctx->queue, ctx->shape_forced ? &ctx->shape : nullptr);
+        const uint32_t* lut = nullptr;
+        DEPIX_TRY(ensure_tables(s));
+        DEPIX_TRY(scale_table(p->scale, s, &lut));
+        const QueueCall c{n, w, h, in_offset, out_offset, d_img, d_out, d_labels, thr, p->subdivide, p->scale,
+                          lut, ctx->graph_a, ctx->graph_b};
+        DEPIX_TRY(queue_prepare(ctx->queue, c, s));
+        if (!ctx->timing) return queue_launch_graph(ctx->queue, s);
+        DEPIX_TRY(queue_reset(ctx->queue, s));
+        static const int kStage[QS_COUNT] = {DEPIX_STAGE_GRAPH, DEPIX_STAGE_HEURISTICS, DEPIX_STAGE_LABELS,
+                                             DEPIX_STAGE_RASTER};
+        for (int st = 0; st < QS_COUNT; st++) {
+            if (st == QS_LABEL && !d_labels) continue;
+            StageTimer t(ctx, kStage[st], st == QS_LABEL ? 3 : 1, s);
+            DEPIX_TRY(queue_launch_stage(ctx->queue, st, s));
+        }
+        return DEPIX_OK;
+    }
+    // uneven frames while capturing, or beyond the mask raster's scales: one
+    // launch per stage and frame
     size_t goff = 0, loff = 0;
     for (int k = 0; k < n; k++) {
         const uint8_t* img = d_img + in_offset[k];
@@ -552,12 +580,39 @@ depix_status depix_context_destroy(depix_context* c)
     cudaFree(c->stage_in);
     cudaFree(c->stage_out);
     cudaFree(c->stage_labels);
+    if (c->queue) queue_runner_destroy(c->queue);
     for (auto& m : c->marks) {
         cudaEventDestroy(m.a);
         cudaEventDestroy(m.b);
     }
     for (auto e : c->spare) cudaEventDestroy(e);
     delete c;
+    return DEPIX_OK;
+}
+
+depix_status depix_context_set_launch_shape(depix_context* c, int gran, int tile_w, int tile_h)
+{
+    if (!c) return arg_fail("NULL context");
+    if (gran == 0) {
+        c->shape_forced = false;
+        return DEPIX_OK;
+    }
+    if (gran != 1 && gran != 2 && gran != 4 && gran != 8) return arg_fail("granularity must be 0, 1, 2, 4 or 8");
+    if (!((tile_w == 32 && tile_h == 32) || (tile_w == 32 && tile_h == 16) || (tile_w == 16 && tile_h == 16)))
+        return arg_fail("raster tile must be 32x32, 32x16 or 16x16");
+    c->shape = QueueShape{{gran, gran, gran, gran}, tile_w, tile_h};
+    c->shape_forced = true;
+    return DEPIX_OK;
+}
+
+depix_status depix_context_launch_shape(depix_context* c, int* gran, int* tile_w, int* tile_h)
+{
+    if (!c) return arg_fail("NULL context");
+    QueueShape sh = c->queue ? queue_last_shape(c->queue) : QueueShape{{0, 0, 0, 0}, 0, 0};
+    if (gran)
+        for (int k = 0; k < QS_COUNT; k++) gran[k] = sh.gran[k];
+    if (tile_w) *tile_w = sh.rtw;
+    if (tile_h) *tile_h = sh.rth;
     return DEPIX_OK;
 }
 

@@ -666,3 +666,41 @@ __device__ __forceinline__ void crossing_mask(const Packed& P, int u, int mlo, i
 }
 
 }  // namespace depix
+
+namespace depix {
+
+// Persistent work loop: the block pulls `gran` tile indices at a time from
+// *counter until `total` is reached and runs body(t) on each; a barrier
+// separates tiles (the bodies reuse shared memory). No block waits on
+// another: a block stops when the counter passes the end.
+template <typename Body>
+__device__ __forceinline__ void queue_loop(int* counter, int total, int gran, Body body)
+{
+    __shared__ int s_first;
+    for (;;) {
+        if (threadIdx.x == 0) s_first = atomicAdd(counter, gran);
+        __syncthreads();
+        const int t0 = s_first;
+        __syncthreads();
+        if (t0 >= total) break;
+        const int t1 = min(t0 + gran, total);
+        for (int t = t0; t < t1; t++) {
+            body(t);
+            __syncthreads();
+        }
+    }
+}
+
+// the frame f with base[f] <= t < base[f + 1]
+__device__ __forceinline__ int queue_frame(const uint32_t* base, int n, uint32_t t)
+{
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(base + mid) <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+}  // namespace depix

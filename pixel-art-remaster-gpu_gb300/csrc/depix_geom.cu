@@ -611,13 +611,11 @@ cudaError_t build_scale_masks(int s, uint32_t* lut, cudaStream_t st)
     return cudaGetLastError();
 }
 
-constexpr int kMTW = 32; // tile width in cells; the height is a template parameter
-
-template <int TH>
+template <int TW, int TH>
 struct MaskTile {
-    static constexpr int GW = kMTW + 2, GH = TH + 2, GN = GW * GH; // cells with their ring
-    static constexpr int BW = kMTW + 6, BH = TH + 6;               // graph, halo 3
-    static constexpr int CW = kMTW + 4, CH = TH + 4;               // pixels, halo 2
+    static constexpr int GW = TW + 2, GH = TH + 2, GN = GW * GH; // cells with their ring
+    static constexpr int BW = TW + 6, BH = TH + 6;               // graph, halo 3
+    static constexpr int CW = TW + 4, CH = TH + 4;               // pixels, halo 2
     uint8_t graph[BH][BW];
     uint32_t pix[CH][CW];
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
@@ -757,12 +755,12 @@ __device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const Ma
     return spill_bits(mnx, mny, mxx, mxy);
 }
 
-template <int LAYOUT, int S, int TH>
-__device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
+template <int LAYOUT, int S, int TW, int TH>
+__device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
                                  uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
                                  int y0)
 {
-    using T = MaskTile<TH>;
+    using T = MaskTile<TW, TH>;
     const int s = S > 0 ? S : scale;
     const MaskGeom G = mask_geom(s);
     const int F = G.F;
@@ -841,8 +839,8 @@ __device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t
     const int ow = w * s;
     const bool vec = ((S == 4 || S == 8) && (ow % 4) == 0 && ((reinterpret_cast<uintptr_t>(out) & 15) == 0));
     const uint32_t blockbits = (s >= 32) ? 0xFFFFFFFFu : ((1u << s) - 1u);
-    for (int q = threadIdx.x; q < kMTW * TH; q += blockDim.x) {
-        int tx = q % kMTW, ty = q / kMTW;
+    for (int q = threadIdx.x; q < TW * TH; q += blockDim.x) {
+        int tx = q % TW, ty = q / TW;
         int ci = x0 + tx, cj = y0 + ty;
         if (ci >= w || cj >= h) continue;
         const int k0 = (ty + 1) * T::GW + (tx + 1);
@@ -920,30 +918,105 @@ __device__ void mask_raster_tile(MaskTile<TH>& M, uint32_t* masks, const uint8_t
 template <int LAYOUT, int S, int TH>
 __global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32_t* lut)
 {
-    __shared__ MaskTile<TH> M;
+    __shared__ MaskTile<32, TH> M;
     extern __shared__ uint32_t masks[];
     size_t z = blockIdx.z;
-    mask_raster_tile<LAYOUT, S, TH>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
-                                    b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut,
-                                    blockIdx.x * kMTW, blockIdx.y * TH);
+    mask_raster_tile<LAYOUT, S, 32, TH>(M, masks, b.img + b.img_stride * z, b.ws, b.graph + b.graph_stride * z,
+                                        b.out + b.out_stride * z, b.w, b.h, b.scale, b.subdivide != 0, lut,
+                                        blockIdx.x * 32, blockIdx.y * TH);
 }
 
 template <int LAYOUT, int S, int TH>
 static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
 {
     MaskGeom g = mask_geom(b.scale);
-    size_t smem = (size_t)MaskTile<TH>::GN * g.F * sizeof(uint32_t);
-    if (smem + sizeof(MaskTile<TH>) > 48 * 1024) {
-        // opt in to more than 48 KB of shared memory in total (a per-device
-        // function attribute; setting it again is harmless)
+    size_t smem = (size_t)MaskTile<32, TH>::GN * g.F * sizeof(uint32_t);
+    if (smem + sizeof(MaskTile<32, TH>) > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_mask_raster<LAYOUT, S, TH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    dim3 grid((b.w + kMTW - 1) / kMTW, (b.h + TH - 1) / TH, nframes);
+    dim3 grid((b.w + 32 - 1) / 32, (b.h + TH - 1) / TH, nframes);
     k_mask_raster<LAYOUT, S, TH><<<grid, 256, smem, s>>>(b, lut);
     return cudaGetLastError();
 }
+
+// ---- uneven batches: the raster as a persistent kernel over a tile queue
+
+template <int S, int TW, int TH>
+__global__ void __launch_bounds__(256) k_raster_queue(QueueBatch q)
+{
+    __shared__ MaskTile<TW, TH> M;
+    extern __shared__ uint32_t masks[];
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_RASTER, (int)H->total[QS_RASTER + raster_shape_index(TW, TH)], q.gran[QS_RASTER], [&](int t) {
+        constexpr int P = QS_RASTER + raster_shape_index(TW, TH);
+        const uint32_t* base = H->base + P * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        const int lt = t - (int)base[f], tx = (fr.w + TW - 1) / TW;
+        mask_raster_tile<DEPIX_LAYOUT_RGBA, S, TW, TH>(M, masks, H->img + fr.in_off, 4 * fr.w, q.graph_b + fr.px_off,
+                                                       H->out + fr.out_off, fr.w, fr.h, q.scale, H->subdivide != 0,
+                                                       q.lut, (lt % tx) * TW, (lt / tx) * TH);
+    });
+}
+
+template <int S, int TW, int TH>
+static size_t raster_queue_smem(int scale)
+{
+    return (size_t)MaskTile<TW, TH>::GN * mask_geom(scale).F * sizeof(uint32_t);
+}
+
+template <int S, int TW, int TH>
+static cudaError_t queue_raster_t(const QueueBatch& q, int blocks, cudaStream_t s)
+{
+    // the shared-memory opt-in is made by raster_queue_occupancy, which the
+    // host calls on each device before any launch or stream capture
+    const size_t smem = raster_queue_smem<S, TW, TH>(q.scale);
+    k_raster_queue<S, TW, TH><<<blocks, 256, smem, s>>>(q);
+    return cudaGetLastError();
+}
+
+template <int S, int TW, int TH>
+static int raster_queue_occupancy(int scale)
+{
+    int nb = 0;
+    const size_t smem = raster_queue_smem<S, TW, TH>(scale);
+    if (smem + sizeof(MaskTile<TW, TH>) > 48 * 1024 &&
+        cudaFuncSetAttribute(k_raster_queue<S, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster_queue<S, TW, TH>, 256, smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+// raster tile variants of the queue path: 32x32, 32x16, 16x16 cells
+#define DEPIX_RQ_DISPATCH(FN, ...)                                                                      \
+    do {                                                                                                \
+        const int sc = q.scale == 4 ? 4 : (q.scale == 8 ? 8 : 0);                                       \
+        if (q.rtw == 32 && q.rth == 32) {                                                               \
+            if (sc == 4) return FN<4, 32, 32>(__VA_ARGS__);                                             \
+            if (sc == 8) return FN<8, 32, 32>(__VA_ARGS__);                                             \
+            return FN<0, 32, 32>(__VA_ARGS__);                                                          \
+        }                                                                                               \
+        if (q.rtw == 32) {                                                                              \
+            if (sc == 4) return FN<4, 32, 16>(__VA_ARGS__);                                             \
+            if (sc == 8) return FN<8, 32, 16>(__VA_ARGS__);                                             \
+            return FN<0, 32, 16>(__VA_ARGS__);                                                          \
+        }                                                                                               \
+        if (sc == 4) return FN<4, 16, 16>(__VA_ARGS__);                                                 \
+        if (sc == 8) return FN<8, 16, 16>(__VA_ARGS__);                                                 \
+        return FN<0, 16, 16>(__VA_ARGS__);                                                              \
+    } while (0)
+
+cudaError_t queue_raster(const QueueBatch& q, int blocks, cudaStream_t s)
+{
+    DEPIX_RQ_DISPATCH(queue_raster_t, q, blocks, s);
+}
+
+int queue_raster_blocks_per_sm(const QueueBatch& q) { DEPIX_RQ_DISPATCH(raster_queue_occupancy, q.scale); }
 
 // 32x32-cell tiles up to scale 4 (more subdivided cells per block to share
 // the work), 32x16 above (the footprint masks grow with the scale)

@@ -292,14 +292,12 @@ __device__ __forceinline__ void s_unite(int* L, int a, int b)
     }
 }
 
-__global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+// union-find inside one 32x32 tile (x0, y0): local roots as global indices
+__device__ void cc_local_tile(const uint8_t* g, int32_t* L, int w, int h, int x0, int y0)
 {
     __shared__ int sl[kLT * kLT];
     __shared__ uint16_t run[kLT * kLT];
     __shared__ uint8_t sg[kLT * kLT];
-    g += frame_stride * blockIdx.z;
-    L += frame_stride * blockIdx.z;
-    const int x0 = blockIdx.x * kLT, y0 = blockIdx.y * kLT;
     for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
         int x = x0 + p % kLT, y = y0 + p / kLT;
         sg[p] = (x < w && y < h) ? g[(size_t)y * w + x] & inside_mask(x, y, w, h) : 0;
@@ -341,17 +339,21 @@ __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, 
     }
 }
 
+__global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+{
+    cc_local_tile(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, blockIdx.x * kLT,
+                  blockIdx.y * kLT);
+}
+
 // unions across tile borders: every set bit whose neighbour lies in another
 // tile (each symmetric pair is seen from both ends; uniting twice is
 // harmless). One thread per border pixel of a tile (4 * 32 - 4 of them).
 constexpr int kLBorder = 4 * kLT - 4;
 
-__global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+// unions of border pixel q of tile `tile` with neighbours in other tiles
+__device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int tiles_x = (w + kLT - 1) / kLT, tiles_y = (h + kLT - 1) / kLT;
-    const int tile = t / kLBorder, q = t % kLBorder;
-    if (tile >= tiles_x * tiles_y) return;
+    const int tiles_x = (w + kLT - 1) / kLT;
     // border position q: bottom row, top row, then left and right columns
     int lx, ly;
     if (q < kLT) { lx = q; ly = 0; }
@@ -360,8 +362,6 @@ __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t fr
     else { lx = kLT - 1; ly = q - (3 * kLT - 2) + 1; }
     const int i = (tile % tiles_x) * kLT + lx, j = (tile / tiles_x) * kLT + ly;
     if (i >= w || j >= h) return;
-    g += frame_stride * blockIdx.z;
-    L += frame_stride * blockIdx.z;
     const int k = j * w + i;
     unsigned node = g[k];
 #pragma unroll
@@ -374,12 +374,136 @@ __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t fr
     }
 }
 
+__global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tiles = ((w + kLT - 1) / kLT) * ((h + kLT - 1) / kLT);
+    if (t / kLBorder >= tiles) return;
+    cc_merge_border(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, t / kLBorder, t % kLBorder);
+}
+
 __global__ void k_cc_flatten(int32_t* L, int n, size_t frame_stride)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     L += frame_stride * blockIdx.z;
     L[k] = uf_find(L, k);
+}
+
+// ------------------------------------------------ uneven batches (queue)
+
+__global__ void __launch_bounds__(256) k_graph_queue(QueueBatch q)
+{
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_GRAPH, (int)H->total[QS_GRAPH], q.gran[QS_GRAPH], [&](int t) {
+        const uint32_t* base = H->base + QS_GRAPH * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        const int lt = t - (int)base[f], tx = (fr.w + kGTW - 1) / kGTW;
+        FrameRef ref{H->img + fr.in_off, fr.w, fr.h, 4 * fr.w, q.graph_a + fr.px_off};
+        graph_tile<DEPIX_LAYOUT_RGBA>(ref, (lt % tx) * kGTW, (lt / tx) * kGTH, H->thr, true);
+    });
+}
+
+__global__ void __launch_bounds__(256) k_heur_queue(QueueBatch q)
+{
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_HEUR, (int)H->total[QS_HEUR], q.gran[QS_HEUR], [&](int t) {
+        const uint32_t* base = H->base + QS_HEUR * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        const int lt = t - (int)base[f], tx = (fr.w + kHTW - 1) / kHTW;
+        heuristics_tile(q.graph_a + fr.px_off, q.graph_b + fr.px_off, fr.w, fr.h, (lt % tx) * kHTW,
+                        (lt / tx) * kHTH);
+    });
+}
+
+__global__ void __launch_bounds__(256) k_label_local_queue(QueueBatch q)
+{
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_LOCAL, (int)H->total[QS_LABEL], q.gran[QS_LABEL], [&](int t) {
+        const uint32_t* base = H->base + QS_LABEL * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        const int lt = t - (int)base[f], tx = (fr.w + kLT - 1) / kLT;
+        cc_local_tile(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h, (lt % tx) * kLT, (lt / tx) * kLT);
+    });
+}
+
+__global__ void __launch_bounds__(128) k_label_merge_queue(QueueBatch q)
+{
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_MERGE, (int)H->total[QS_LABEL], q.gran[QS_LABEL], [&](int t) {
+        const uint32_t* base = H->base + QS_LABEL * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        for (int b = threadIdx.x; b < kLBorder; b += blockDim.x)
+            cc_merge_border(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h, t - (int)base[f], b);
+    });
+}
+
+__global__ void __launch_bounds__(256) k_label_flatten_queue(QueueBatch q)
+{
+    const QueueHeader* H = q.hdr;
+    const int n = H->n;
+    queue_loop(q.counters + QC_FLATTEN, (int)H->total[QS_LABEL], q.gran[QS_LABEL], [&](int t) {
+        const uint32_t* base = H->base + QS_LABEL * (n + 1);
+        const int f = queue_frame(base, n, (uint32_t)t);
+        const QueueFrame fr = H->frames[f];
+        const int lt = t - (int)base[f], tx = (fr.w + kLT - 1) / kLT;
+        const int x0 = (lt % tx) * kLT, y0 = (lt / tx) * kLT;
+        int32_t* L = H->labels + fr.px_off;
+        for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
+            const int x = x0 + p % kLT, y = y0 + p / kLT;
+            if (x < fr.w && y < fr.h) L[y * fr.w + x] = uf_find(L, y * fr.w + x);
+        }
+    });
+}
+
+cudaError_t queue_graph(const QueueBatch& q, int blocks, cudaStream_t s)
+{
+    k_graph_queue<<<blocks, 256, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+cudaError_t queue_heuristics(const QueueBatch& q, int blocks, cudaStream_t s)
+{
+    k_heur_queue<<<blocks, 256, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+cudaError_t queue_labels(const QueueBatch& q, int blocks, cudaStream_t s)
+{
+    k_label_local_queue<<<blocks, 256, 0, s>>>(q);
+    k_label_merge_queue<<<blocks, 128, 0, s>>>(q);
+    k_label_flatten_queue<<<blocks, 256, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+static_assert(kQGraphTW == kGTW && kQGraphTH == kGTH, "graph queue tile");
+static_assert(kQHeurTW == kHTW && kQHeurTH == kHTH, "heuristics queue tile");
+static_assert(kQLabelT == kLT, "label queue tile");
+
+template <typename K>
+static int occupancy(K kernel, int threads)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0) != cudaSuccess) return 0;
+    return nb;
+}
+
+int queue_blocks_per_sm(int stage, const QueueBatch& q)
+{
+    switch (stage) {
+    case QS_GRAPH: return occupancy(k_graph_queue, 256);
+    case QS_HEUR: return occupancy(k_heur_queue, 256);
+    case QS_LABEL: return std::min(occupancy(k_label_local_queue, 256), occupancy(k_label_flatten_queue, 256));
+    default: return queue_raster_blocks_per_sm(q);
+    }
 }
 
 __global__ void k_yuv_words(const uint8_t* px3, size_t n, uint32_t* out)

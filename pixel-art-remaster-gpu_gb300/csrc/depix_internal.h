@@ -50,17 +50,104 @@ struct RasterBatch {
     int subdivide;
 };
 
-// One frame of a variable-size batch (device array entry).
-struct BatchFrame {
-    uint64_t in_off;  // image offset (bytes) in the batch input
-    uint64_t out_off; // raster offset (bytes) in the batch output
-    uint64_t px_off;  // offset (pixels) of the frame's graph in the scratch graphs
+// ------------------------------------------------ uneven batches (queue)
+//
+// Frames of any sizes in one launch per stage: per-frame descriptors and,
+// per stage, the prefix sums of the frames' tile counts live in device
+// memory; persistent kernels pull tile indices from a counter and find a
+// tile's frame by binary search over the prefix.
+enum QueueStage { QS_GRAPH = 0, QS_HEUR = 1, QS_LABEL = 2, QS_RASTER = 3, QS_COUNT = 4 };
+enum QueueCounter { QC_GRAPH = 0, QC_HEUR, QC_LOCAL, QC_MERGE, QC_FLATTEN, QC_RASTER, QC_COUNT };
+
+struct QueueFrame {
+    uint64_t in_off;  // bytes into the batch input (RGBA8, rows 4*w bytes)
+    uint64_t out_off; // bytes into the batch raster output
+    uint64_t px_off;  // pixels into the scratch graphs and the labels
     int w, h;
-    int tile_base_graph; // first graph-stage tile index of this frame
-    int tile_base_heur;  // first heuristics-stage tile index
-    int tile_base_rast;  // first raster-stage tile index
-    int pad;
 };
+
+// Per-call descriptor block, copied to the device in one piece: this header,
+// then the QS_COUNT prefix arrays (n + 1 entries each), then the frames.
+struct QueueHeader {
+    int n;            // frames in this batch
+    uint32_t thr;     // packed similarity thresholds
+    int subdivide;
+    int pad_;
+    const uint8_t* img;
+    uint8_t* out;
+    int32_t* labels;
+    const QueueFrame* frames;
+    const uint32_t* base;     // base[prefix * (n + 1) + f]: first tile of frame f
+    uint32_t total[6];        // tiles per prefix (kQPrefixes)
+};
+
+// Kernel parameters: fixed for a context, a scale and a launch shape, so a
+// captured graph replays them for every batch.
+struct QueueBatch {
+    const QueueHeader* hdr;
+    int* counters;        // QC_COUNT tile counters, zeroed before each batch
+    uint8_t* graph_a;     // after graph + trivial
+    uint8_t* graph_b;     // resolved
+    const uint32_t* lut;  // scale table
+    int scale;
+    int gran[QS_COUNT];   // tiles pulled per counter step, per stage
+    int rtw, rth;         // raster tile (cells)
+};
+
+// tiles of a frame per stage; the raster has three tile shapes, each with its
+// own prefix (QS_RASTER + shape index), so a batch can be raster-timed in
+// every shape without new descriptors
+constexpr int kQGraphTW = 64, kQGraphTH = 8, kQHeurTW = 64, kQHeurTH = 16, kQLabelT = 32;
+constexpr int kQRasterShapes = 3;
+constexpr int kQPrefixes = QS_RASTER + kQRasterShapes;
+static_assert(kQPrefixes == 6, "QueueHeader::total");
+constexpr int kQRasterTW[kQRasterShapes] = {32, 32, 16}, kQRasterTH[kQRasterShapes] = {32, 16, 16};
+__host__ __device__ constexpr int raster_shape_index(int tw, int th)
+{
+    return (tw == 32 && th == 32) ? 0 : (tw == 32 ? 1 : 2);
+}
+
+class QueueRunner;
+struct QueueCall {
+    int n;
+    const int* w;
+    const int* h;
+    const uint64_t* in_off;
+    const uint64_t* out_off;
+    const uint8_t* img;
+    uint8_t* out;
+    int32_t* labels;      // NULL: no label stage
+    uint32_t thr;
+    int subdivide, scale;
+    const uint32_t* lut;
+    uint8_t* graph_a;
+    uint8_t* graph_b;
+};
+// Launch shape of the queue path: granularity per stage and raster tile.
+struct QueueShape {
+    int gran[QS_COUNT];
+    int rtw, rth;
+};
+depix_status queue_runner_create(int cap, QueueRunner** out);
+void queue_runner_destroy(QueueRunner* r);
+// fills a pinned descriptor slot for the call, copies it to the device on s
+// and picks the launch shape (forced, tuned for the batch's size bucket, or
+// tuned now by timing the candidates on s)
+depix_status queue_prepare(QueueRunner* r, const QueueCall& c, cudaStream_t s);
+// the prepared batch as one graph replay, or stage by stage
+depix_status queue_launch_graph(QueueRunner* r, cudaStream_t s);
+depix_status queue_reset(QueueRunner* r, cudaStream_t s);
+depix_status queue_launch_stage(QueueRunner* r, int stage, cudaStream_t s);
+bool queue_has_labels(const QueueRunner* r);
+void queue_force_shape(QueueRunner* r, const QueueShape* shape); // NULL: tune
+QueueShape queue_last_shape(const QueueRunner* r);
+
+cudaError_t queue_graph(const QueueBatch& q, int blocks, cudaStream_t s);
+cudaError_t queue_heuristics(const QueueBatch& q, int blocks, cudaStream_t s);
+cudaError_t queue_labels(const QueueBatch& q, int blocks, cudaStream_t s);
+cudaError_t queue_raster(const QueueBatch& q, int blocks, cudaStream_t s);
+int queue_blocks_per_sm(int stage, const QueueBatch& q);
+int queue_raster_blocks_per_sm(const QueueBatch& q);
 
 // text returned by depix_last_error() on this thread
 void set_last_error(const std::string& msg);

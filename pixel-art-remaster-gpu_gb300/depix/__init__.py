@@ -72,6 +72,8 @@ def lib():
         _sig(L, "depix_batch_host", [_vp, _i, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, P, _vp, ctypes.c_size_t,
                                      _vp, _vp])
         _sig(L, "depix_context_set_timing", [_vp, _i])
+        _sig(L, "depix_context_set_launch_shape", [_vp, _i, _i, _i])
+        _sig(L, "depix_context_launch_shape", [_vp, _vp, _vp, _vp])
         _sig(L, "depix_context_stage_times", [_vp, _vp, _vp, _vp])
         _sig(L, "depix_launch_kernel_compat", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, _i, P], _vp)
         _sig(L, "launch_kernel", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, ctypes.c_bool], _vp)
@@ -205,6 +207,19 @@ class Context:
         _check(lib().depix_batch_host(self.handle, n, W, H, I, O, ptr(h_img), in_bytes, ctypes.byref(p),
                                       ptr(h_out), out_bytes, ptr(h_labels), stream_ptr(stream)),
                "depix_batch_host")
+
+    def set_launch_shape(self, gran=0, tile_w=32, tile_h=32):
+        """Queue-path shape for uneven batches; gran 0 returns to tuning."""
+        _check(lib().depix_context_set_launch_shape(self.handle, gran, tile_w, tile_h),
+               "depix_context_set_launch_shape")
+
+    def launch_shape(self):
+        """(gran per stage, raster tile w, h) of the last queue-path batch."""
+        g = (ctypes.c_int * 4)()
+        tw, th = ctypes.c_int(), ctypes.c_int()
+        _check(lib().depix_context_launch_shape(self.handle, g, ctypes.byref(tw), ctypes.byref(th)),
+               "depix_context_launch_shape")
+        return tuple(g), tw.value, th.value
 
     def set_timing(self, on=True):
         _check(lib().depix_context_set_timing(self.handle, int(bool(on))), "depix_context_set_timing")

@@ -60,6 +60,8 @@ def test_bad_arguments_are_rejected_before_cuda(L):
     h = ctypes.c_void_p()
     assert L.depix_context_create(ctypes.byref(h), 0, 1) == 1
     assert b"capacity" in L.depix_last_error()
+    # launch shape of a missing context
+    assert L.depix_context_set_launch_shape(None, 1, 32, 32) == 1
 
 
 def test_default_params(L):
