@@ -230,6 +230,56 @@ depix_status depix_context_set_timing(depix_context* ctx, int enable);
 depix_status depix_context_stage_times(depix_context* ctx, double* ms, long long* launches, long long* calls);
 
 /* ---------------------------------------------------------------------
+ * Spline refinement (no reference counterpart: the reference's frame path
+ * ends at the VBO fill). Node positions of the colour boundaries are
+ * optimised on the GPU with Adam against curvature, deviation and a soft
+ * coverage loss at the output scale; the topology is frozen at setup.
+ * --------------------------------------------------------------------- */
+
+typedef struct depix_refiner depix_refiner;
+typedef struct depix_refine_params {
+    float w_curvature; /* 1.0: mean squared second difference of the Chaikin points at free nodes */
+    float w_deviation; /* 0.25: mean squared distance of free nodes from their start */
+    float w_coverage;  /* 1.0: mean squared RGB error of the soft raster against the x scale target */
+    float sigma;       /* 0.5: coverage Gaussian, output pixels (fixed at setup) */
+    float lr;          /* 0.05: Adam step, source pixels */
+    int steps;         /* 200 */
+} depix_refine_params;
+
+void depix_refine_default_params(depix_refine_params* p);
+/* Scratch for frames of up to max_pixels pixels. */
+depix_status depix_refiner_create(depix_refiner** r, size_t max_pixels);
+depix_status depix_refiner_destroy(depix_refiner* r);
+/* Extracts and freezes one frame's topology from its image and resolved
+ * graph (p: thresholds of the curve test, output scale 1..12): nodes, curve
+ * edges, Chaikin segments, the output samples near each segment and their
+ * targets. Synchronises the stream (reads counts back). */
+depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, int h, int widthstep,
+                                depix_layout layout, const uint8_t* d_graph, const depix_params* p,
+                                const depix_refine_params* rp, depix_stream s);
+/* nodes, free nodes, curve edges, segment slots, assigned samples */
+depix_status depix_refine_counts(depix_refiner* r, long long counts[5]);
+/* The frozen topology to host arrays (any may be NULL): node quarter-pixel
+ * coordinates (2 per node), flags (bit 0 pinned, 1 frame, 2 corner, degree
+ * << 4), neighbours of degree-2 nodes (2 per node, -1 otherwise), edges (u,
+ * v, left cell, right cell), segment slots (3 nodes, type), slot colours
+ * (left, right as 0xBBGGRR) and samples (output index, slot). Synchronous. */
+depix_status depix_refine_export(depix_refiner* r, int32_t* node_q, int32_t* node_flags, int32_t* node_nbr,
+                                 int32_t* edges, int32_t* segs, uint32_t* seg_colors, int32_t* samples);
+/* Start positions (float x, y per node, source pixels) to d_pos. */
+depix_status depix_refine_initial(depix_refiner* r, float* d_pos, depix_stream s);
+/* Energy terms (curvature, deviation, coverage, total) at d_pos and, when
+ * d_grad is set, dE/d position per node (zero at pinned nodes): the adjoint.
+ * Synchronous. */
+depix_status depix_refine_energy_grad(depix_refiner* r, const depix_refine_params* p, const float* d_pos,
+                                      float* d_grad, double energy[4], depix_stream s);
+/* p->steps Adam steps (beta 0.9 / 0.999, eps 1e-8) from d_pos (NULL: the
+ * start positions); the result goes back to d_pos when set. Energies before
+ * and after when the pointers are set (those evaluations synchronise). */
+depix_status depix_refine_run(depix_refiner* r, const depix_refine_params* p, float* d_pos, double before[4],
+                              double after[4], depix_stream s);
+
+/* ---------------------------------------------------------------------
  * Drop-in replacement of the reference's frame driver.
  * --------------------------------------------------------------------- */
 

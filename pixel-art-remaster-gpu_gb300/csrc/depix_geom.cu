@@ -188,6 +188,14 @@ cudaError_t init_tables(cudaStream_t s)
     return cudaGetLastError();
 }
 
+cudaError_t hull_table_address(const uint64_t** out)
+{
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_hull_lut);
+    *out = static_cast<const uint64_t*>(p);
+    return e;
+}
+
 cudaError_t copy_tables(uint64_t* hull, uint64_t* tri)
 {
     cudaError_t e = cudaMemcpyFromSymbol(hull, g_hull_lut, sizeof(g_hull_lut));

@@ -164,6 +164,8 @@ cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, uint32_t* out, cudaSt
 // geometry stage
 cudaError_t init_tables(cudaStream_t s);
 cudaError_t copy_tables(uint64_t* hull, uint64_t* tri);
+// device address of the per-pattern hull table (this device)
+cudaError_t hull_table_address(const uint64_t** out);
 cudaError_t launch_cells(const uint8_t* g, int w, int h, float* diagram, int* ec, cudaStream_t s);
 cudaError_t launch_subdivide(const uint8_t* img, int w, int h, int ws, int layout, const uint8_t* g,
                              const float* snap, const int* ec_snap, float* diagram, int* ec, cudaStream_t s);

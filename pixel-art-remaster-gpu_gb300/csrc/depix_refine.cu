@@ -1,0 +1,1159 @@
+// depix_refine.cu -- spline refinement: node positions of the colour
+// boundaries optimised against curvature, deviation and a soft-coverage
+// raster loss, with a hand-written adjoint.
+//
+// The reference has no such stage (its frame path ends at the VBO fill,
+// kernel.cu:439-520). Its definition here:
+//
+// Topology, extracted once per frame and frozen:
+//   * cells are the hulls of the resolved graph's cell patterns (the hull
+//     table); split at every hull vertex lying inside an edge, the cells'
+//     edges pair up exactly with reversed twins in 8-neighbour cells;
+//   * a split edge whose twin belongs to a dissimilar cell is a curve edge,
+//     kept once (from the lower-indexed cell, along its counter-clockwise
+//     hull: its colour on the left);
+//   * nodes are curve-edge vertices in global quarter-pixel units, numbered
+//     in vertex-grid order; pinned when not of degree 2, on an edge without
+//     a twin (the frame), or where the two edges turn by 90 degrees or more;
+//   * one Chaikin round gives the segments: the middle of each edge (slot
+//     3e+1), the piece from a pinned end to the first cut point (3e, 3e+2)
+//     and the cut corner of each free node (3E + node);
+//   * every output sample within 1.5 output pixels of a segment is assigned
+//     to the nearest one (exact integer distances, one rounded division;
+//     ties to the lower slot).
+// Energy (every term a mean): w_curv * 1/F sum_free |a - 2p + b|^2 / 8
+//   + w_dev * 1/F sum_free |p - p0|^2
+//   + w_cov * 1/(3 Ws Hs) sum_samples sum_rgb ((r - t)/255)^2,
+//   r = cR + (cL - cR) Phi(d / sigma), d the sample's signed distance from
+//   its segment's line, t the nearest-neighbour target under the same
+//   Gaussian coverage. The adjoint recomputes each segment's Chaikin points
+//   from the nodes in the backward pass instead of storing them.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "depix_internal.h"
+
+namespace depix {
+
+namespace {
+
+constexpr int kBand = 48;          // 1.5 output pixels in 1/(32 s) source pixel
+constexpr int kMaxRefineScale = 12;
+enum SegType { SEG_NONE = 0, SEG_MID = 1, SEG_PIN_U = 2, SEG_PIN_V = 3, SEG_CORNER = 4 };
+// weights (x4) of a segment's ends over its three node slots, per type
+__constant__ int8_t c_seg_wa[5][3] = {{0, 0, 0}, {3, 1, 0}, {4, 0, 0}, {1, 3, 0}, {1, 3, 0}};
+__constant__ int8_t c_seg_wb[5][3] = {{0, 0, 0}, {1, 3, 0}, {3, 1, 0}, {0, 4, 0}, {0, 3, 1}};
+
+// vertex grid word: bit 0 a hull vertex, bit 1 on an edge without a twin,
+// bits 8.. the number of curve edges
+constexpr uint32_t kVUsed = 1, kVFrame = 2;
+constexpr int kNoSeg = 0x7F7F7F7F; // a byte fill of 0x7F: no segment
+constexpr int kDegShift = 8;
+
+struct Geo {
+    const uint8_t* img;
+    int ws, layout;
+    const uint8_t* g;
+    int w, h;
+    int gw, gh;         // vertex grid: (4w + 3) x (4h + 3), origin at quarter (-1, -1)
+    const uint64_t* lut;
+    uint32_t thr;
+};
+
+__device__ __forceinline__ uint64_t cell_hull(const Geo& G, int idx)
+{
+    const int n = G.w * G.h;
+    const unsigned node = G.g[idx];
+    const unsigned left = idx > 0 ? G.g[idx - 1] : 0u;
+    const unsigned right = idx + 1 < n ? G.g[idx + 1] : 0u;
+    return __ldg(&G.lut[cell_pattern(node, left, right)]);
+}
+
+// hull vertex t in global quarter units
+__device__ __forceinline__ int qvx(uint64_t e, int t, int i) { return 4 * i + (int)((e >> (4 + 6 * t)) & 7u) - 1; }
+__device__ __forceinline__ int qvy(uint64_t e, int t, int j) { return 4 * j + (int)((e >> (7 + 6 * t)) & 7u) - 1; }
+__device__ __forceinline__ int vindex(const Geo& G, int x, int y) { return (y + 1) * G.gw + (x + 1); }
+
+__device__ __forceinline__ int igcd(int a, int b)
+{
+    a = abs(a);
+    b = abs(b);
+    while (b) {
+        int t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// v -> u lies on p -> q in the same direction
+__device__ __forceinline__ bool reversed_on(int px, int py, int qx, int qy, int ux, int uy, int vx, int vy)
+{
+    const int ex = qx - px, ey = qy - py;
+    if (ex * (vy - py) - ey * (vx - px) != 0 || ex * (uy - py) - ey * (ux - px) != 0) return false;
+    if (ex * (ux - vx) + ey * (uy - vy) <= 0) return false;
+    const int L = ex * ex + ey * ey;
+    const int tv = ex * (vx - px) + ey * (vy - py), tu = ex * (ux - px) + ey * (uy - py);
+    return tv >= 0 && tu <= L;
+}
+
+__device__ __forceinline__ uint32_t cell_word(const Geo& G, int i, int j)
+{
+    return word_of_bgr(load_bgr(G.img, G.ws, G.layout, i, j));
+}
+
+// Walks the split edges of cell idx. For each: owner direction of the twin
+// (-1: none) and the twin cell. fn(ux, uy, vx, vy, owner, B).
+template <typename Fn>
+__device__ void walk_split_edges(const Geo& G, const uint32_t* vgrid, int idx, Fn fn)
+{
+    const int i = idx % G.w, j = idx / G.w;
+    const uint64_t e = cell_hull(G, idx);
+    const int k = (int)(e & 0xF);
+    uint64_t nh[8];
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+        const int ni = i + dir_di(d), nj = j + dir_dj(d);
+        nh[d] = (ni >= 0 && ni < G.w && nj >= 0 && nj < G.h) ? cell_hull(G, nj * G.w + ni) : 0ull;
+    }
+    for (int t = 0; t < k; t++) {
+        const int t1 = t + 1 == k ? 0 : t + 1;
+        const int ax = qvx(e, t, i), ay = qvy(e, t, j), bx = qvx(e, t1, i), by = qvy(e, t1, j);
+        const int gcd = igcd(bx - ax, by - ay);
+        const int sx = (bx - ax) / gcd, sy = (by - ay) / gcd;
+        int px = ax, py = ay;
+        for (int st = 1; st <= gcd; st++) {
+            const int cx = ax + st * sx, cy = ay + st * sy;
+            if (st < gcd && !(vgrid[vindex(G, cx, cy)] & kVUsed)) continue;
+            int owner = -1;
+            for (int d = 0; d < 8 && owner < 0; d++) {
+                const uint64_t ne = nh[d];
+                const int nk = (int)(ne & 0xF);
+                const int ni = i + dir_di(d), nj = j + dir_dj(d);
+                for (int s = 0; s < nk; s++) {
+                    const int s1 = s + 1 == nk ? 0 : s + 1;
+                    if (reversed_on(qvx(ne, s, ni), qvy(ne, s, nj), qvx(ne, s1, ni), qvy(ne, s1, nj), px, py, cx, cy)) {
+                        owner = d;
+                        break;
+                    }
+                }
+            }
+            const int B = owner < 0 ? -1 : (j + dir_dj(owner)) * G.w + (i + dir_di(owner));
+            fn(px, py, cx, cy, owner, B);
+            px = cx;
+            py = cy;
+        }
+    }
+}
+
+__global__ void k_rf_mark_vertices(Geo G, uint32_t* vgrid)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G.w * G.h) return;
+    const int i = idx % G.w, j = idx / G.w;
+    const uint64_t e = cell_hull(G, idx);
+    const int k = (int)(e & 0xF);
+    for (int t = 0; t < k; t++) atomicOr(&vgrid[vindex(G, qvx(e, t, i), qvy(e, t, j))], kVUsed);
+}
+
+// pass 0: curve edges per cell, and the frame marks
+__global__ void k_rf_count_edges(Geo G, uint32_t* vgrid, int* count)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G.w * G.h) return;
+    const int i = idx % G.w, j = idx / G.w;
+    const uint32_t me = cell_word(G, i, j);
+    int c = 0;
+    walk_split_edges(G, vgrid, idx, [&](int ux, int uy, int vx, int vy, int owner, int B) {
+        if (owner < 0) {
+            atomicOr(&vgrid[vindex(G, ux, uy)], kVFrame);
+            atomicOr(&vgrid[vindex(G, vx, vy)], kVFrame);
+        } else if (B > idx && !similar(me, cell_word(G, B % G.w, B / G.w), G.thr)) {
+            c++;
+        }
+    });
+    count[idx] = c;
+}
+
+// pass 1: the curve edges at their offsets; degrees and up to two
+// neighbours (vertex, edge) per vertex
+__global__ void k_rf_emit_edges(Geo G, uint32_t* vgrid, const int* off, int4* edges, int2* nb_v, int2* nb_e)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G.w * G.h) return;
+    const int i = idx % G.w, j = idx / G.w;
+    const uint32_t me = cell_word(G, i, j);
+    int o = off[idx];
+    walk_split_edges(G, vgrid, idx, [&](int ux, int uy, int vx, int vy, int owner, int B) {
+        if (owner < 0 || B <= idx || similar(me, cell_word(G, B % G.w, B / G.w), G.thr)) return;
+        const int u = vindex(G, ux, uy), v = vindex(G, vx, vy);
+        edges[o] = make_int4(u, v, idx, B);
+        const uint32_t su = atomicAdd(&vgrid[u], 1u << kDegShift) >> kDegShift;
+        const uint32_t sv = atomicAdd(&vgrid[v], 1u << kDegShift) >> kDegShift;
+        if (su < 2) {
+            (&nb_v[u].x)[su] = v;
+            (&nb_e[u].x)[su] = o;
+        }
+        if (sv < 2) {
+            (&nb_v[v].x)[sv] = u;
+            (&nb_e[v].x)[sv] = o;
+        }
+        o++;
+    });
+}
+
+__global__ void k_rf_node_flags(const uint32_t* vgrid, int nv, int* is_node)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nv) is_node[v] = (vgrid[v] >> kDegShift) > 0;
+}
+
+struct NodeOut {
+    int2* q;        // quarter coordinates
+    int* flags;     // bit 0 pinned, 1 frame, 2 corner; degree << 4
+    int2* nbr;      // neighbours of degree-2 nodes (ascending), else -1
+    int2* nbr_edge; // the edges to them
+    float2* pos0;
+};
+
+__global__ void k_rf_nodes(Geo G, const uint32_t* vgrid, const int* nid, const int2* nb_v, const int2* nb_e, NodeOut N)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= G.gw * G.gh) return;
+    const uint32_t word = vgrid[v];
+    const int deg = (int)(word >> kDegShift);
+    if (deg == 0) return;
+    const int k = nid[v];
+    const int x = v % G.gw - 1, y = v / G.gw - 1;
+    int f = min(deg, 15) << 4;
+    if (word & kVFrame) f |= 2;
+    int2 nb = make_int2(-1, -1), ne = make_int2(-1, -1);
+    if (deg == 2) {
+        int a = nid[nb_v[v].x], b = nid[nb_v[v].y];
+        int ea = nb_e[v].x, eb = nb_e[v].y;
+        const int va = nb_v[v].x, vb = nb_v[v].y;
+        int vax = va % G.gw - 1, vay = va / G.gw - 1, vbx = vb % G.gw - 1, vby = vb / G.gw - 1;
+        if (a > b) {
+            int t = a; a = b; b = t;
+            t = ea; ea = eb; eb = t;
+            t = vax; vax = vbx; vbx = t;
+            t = vay; vay = vby; vby = t;
+        }
+        nb = make_int2(a, b);
+        ne = make_int2(ea, eb);
+        if ((x - vax) * (vbx - x) + (y - vay) * (vby - y) <= 0) f |= 4;
+    }
+    if (deg != 2 || (f & 6)) f |= 1;
+    N.q[k] = make_int2(x, y);
+    N.flags[k] = f;
+    N.nbr[k] = nb;
+    N.nbr_edge[k] = ne;
+    N.pos0[k] = make_float2(0.25f * x, 0.25f * y);
+}
+
+struct SegOut {
+    int4* seg;    // n0, n1, n2, type
+    uint2* col;   // left, right RGB (0xBBGGRR)
+};
+
+__device__ __forceinline__ uint32_t cell_rgb(const Geo& G, int idx)
+{
+    const uint32_t c = load_bgr(G.img, G.ws, G.layout, idx % G.w, idx / G.w); // b0 | b1 << 8 | b2 << 16
+    // reference bytes (b0, b1, b2) = (B, G, R) -> R | G << 8 | B << 16
+    return ((c >> 16) & 0xFFu) | (c & 0xFF00u) | ((c & 0xFFu) << 16);
+}
+
+// segment slots: 3 per edge, then one per node
+__global__ void k_rf_segments(Geo G, const int* nid, int4* edges, int E, int Nn, const int* flags, const int2* nbr,
+                              const int2* nbr_edge, SegOut S)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < E) {
+        int4 ed = edges[t];
+        const int u = nid[ed.x], v = nid[ed.y];
+        const uint2 col = make_uint2(cell_rgb(G, ed.z), cell_rgb(G, ed.w));
+        const bool pu = flags[u] & 1, pv = flags[v] & 1;
+        S.seg[3 * t] = pu ? make_int4(u, v, -1, SEG_PIN_U) : make_int4(-1, -1, -1, SEG_NONE);
+        S.seg[3 * t + 1] = make_int4(u, v, -1, SEG_MID);
+        S.seg[3 * t + 2] = pv ? make_int4(u, v, -1, SEG_PIN_V) : make_int4(-1, -1, -1, SEG_NONE);
+        S.col[3 * t] = S.col[3 * t + 1] = S.col[3 * t + 2] = col;
+    } else if (t < E + Nn) {
+        const int p = t - E;
+        const int s = 3 * E + p;
+        if (flags[p] & 1) {
+            S.seg[s] = make_int4(-1, -1, -1, SEG_NONE);
+            S.col[s] = make_uint2(0, 0);
+            return;
+        }
+        const int a = nbr[p].x, b = nbr[p].y;
+        const int e = nbr_edge[p].x; // the edge between a and p
+        const int4 ed = edges[e];
+        const uint32_t l = cell_rgb(G, ed.z), r = cell_rgb(G, ed.w);
+        const bool flip = nid[ed.x] != a; // stored as p -> a
+        S.seg[s] = make_int4(a, p, b, SEG_CORNER);
+        S.col[s] = flip ? make_uint2(r, l) : make_uint2(l, r);
+    }
+}
+
+// exact segment ends at the start, in 1/(32 s) source pixel
+__device__ __forceinline__ void seg_ends(const int4 sg, const int2* q, int scale, long long& ax, long long& ay,
+                                         long long& bx, long long& by)
+{
+    ax = ay = bx = by = 0;
+    const int nodes[3] = {sg.x, sg.y, sg.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (nodes[k] < 0) continue;
+        const int2 p = q[nodes[k]];
+        ax += (long long)c_seg_wa[sg.w][k] * p.x;
+        ay += (long long)c_seg_wa[sg.w][k] * p.y;
+        bx += (long long)c_seg_wb[sg.w][k] * p.x;
+        by += (long long)c_seg_wb[sg.w][k] * p.y;
+    }
+    const long long m = 2 * scale; // weights x4, quarter -> 1/(32 s): x 8 s / 4
+    ax *= m;
+    ay *= m;
+    bx *= m;
+    by *= m;
+}
+
+__device__ __forceinline__ double seg_dist2(long long ax, long long ay, long long bx, long long by, long long X,
+                                            long long Y)
+{
+    const long long ex = bx - ax, ey = by - ay, wx = X - ax, wy = Y - ay;
+    const long long L = ex * ex + ey * ey, dot = ex * wx + ey * wy;
+    if (dot <= 0) return (double)(wx * wx + wy * wy);
+    if (dot >= L) return (double)((X - bx) * (X - bx) + (Y - by) * (Y - by));
+    const long long cr = ex * wy - ey * wx;
+    return __ddiv_rn((double)(cr * cr), (double)L);
+}
+
+__device__ __forceinline__ long long floor_div_ll(long long a, long long b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// samples of a segment's box (+ band): fn(sample index, d2)
+template <typename Fn>
+__device__ void seg_samples(const int4 sg, const int2* q, int scale, int ow, int oh, Fn fn)
+{
+    long long ax, ay, bx, by;
+    seg_ends(sg, q, scale, ax, ay, bx, by);
+    // sample Xo sits at 16 (2 Xo + 1)
+    const long long x0 = max(0LL, -floor_div_ll(-(min(ax, bx) - kBand - 16), 32));
+    const long long x1 = min((long long)ow - 1, floor_div_ll(max(ax, bx) + kBand - 16, 32));
+    const long long y0 = max(0LL, -floor_div_ll(-(min(ay, by) - kBand - 16), 32));
+    const long long y1 = min((long long)oh - 1, floor_div_ll(max(ay, by) + kBand - 16, 32));
+    for (long long yo = y0; yo <= y1; yo++)
+        for (long long xo = x0; xo <= x1; xo++) {
+            const double d2 = seg_dist2(ax, ay, bx, by, 16 * (2 * xo + 1), 16 * (2 * yo + 1));
+            if (d2 <= (double)(kBand * kBand)) fn((int)(yo * ow + xo), d2);
+        }
+}
+
+__global__ void k_rf_assign_dist(const int4* seg, int S, const int2* q, int scale, int ow, int oh,
+                                 unsigned long long* best)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int4 sg = seg[s];
+    if (sg.w == SEG_NONE) return;
+    seg_samples(sg, q, scale, ow, oh, [&](int x, double d2) {
+        atomicMin(&best[x], (unsigned long long)__double_as_longlong(d2));
+    });
+}
+
+__global__ void k_rf_assign_seg(const int4* seg, int S, const int2* q, int scale, int ow, int oh,
+                                const unsigned long long* best, int* bseg)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int4 sg = seg[s];
+    if (sg.w == SEG_NONE) return;
+    seg_samples(sg, q, scale, ow, oh, [&](int x, double d2) {
+        if ((unsigned long long)__double_as_longlong(d2) == best[x]) atomicMin(&bseg[x], s);
+    });
+}
+
+__global__ void k_rf_count_samples(const int* bseg, int n, int* seg_count)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < n && bseg[x] != kNoSeg) atomicAdd(&seg_count[bseg[x]], 1);
+}
+
+__global__ void k_rf_scatter_samples(const int* bseg, int n, const int* seg_off, int* cursor, int* samp)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n || bseg[x] == kNoSeg) return;
+    const int s = bseg[x];
+    samp[seg_off[s] + atomicAdd(&cursor[s], 1)] = x;
+}
+
+__global__ void k_rf_count_free(const int* flags, int n, int* out)
+{
+    __shared__ int c;
+    if (threadIdx.x == 0) c = 0;
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && !(flags[k] & 1)) atomicAdd(&c, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && c) atomicAdd(out, c);
+}
+
+// each segment's samples in ascending order (summation order fixed)
+__global__ void k_rf_sort_samples(const int* seg_off, int S, int* samp)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int a = seg_off[s], b = seg_off[s + 1];
+    for (int i = a + 1; i < b; i++) {
+        const int v = samp[i];
+        int j = i - 1;
+        while (j >= a && samp[j] > v) {
+            samp[j + 1] = samp[j];
+            j--;
+        }
+        samp[j + 1] = v;
+    }
+}
+
+// the nearest-neighbour target under the coverage Gaussian, per sample
+__global__ void k_rf_targets(Geo G, int scale, double sig, const int* samp, int M, float4* tgt)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const int ow = G.w * scale;
+    const int xo = samp[m] % ow, yo = samp[m] / ow;
+    const double x = (xo + 0.5) / scale, y = (yo + 0.5) / scale;
+    const int ix = xo / scale, iy = yo / scale;
+    double r = 0, g = 0, b = 0;
+    for (int dj = -1; dj <= 1; dj++) {
+        const int jj = iy + dj;
+        if (jj < 0 || jj >= G.h) continue;
+        const double cy = normcdf((y - jj) / sig) - normcdf((y - jj - 1) / sig);
+        for (int di = -1; di <= 1; di++) {
+            const int ii = ix + di;
+            if (ii < 0 || ii >= G.w) continue;
+            const double cx = normcdf((x - ii) / sig) - normcdf((x - ii - 1) / sig);
+            const uint32_t c = cell_rgb(G, jj * G.w + ii);
+            r += cx * cy * (double)(c & 0xFF);
+            g += cx * cy * (double)((c >> 8) & 0xFF);
+            b += cx * cy * (double)((c >> 16) & 0xFF);
+        }
+    }
+    tgt[m] = make_float4((float)r, (float)g, (float)b, 0.f);
+}
+
+// ---------------------------------------------------------------- scans
+
+constexpr int kScanBlock = 1024, kScanItems = 4, kScanTile = kScanBlock * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int s = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_sums[lane] = s; // inclusive
+    }
+    __syncthreads();
+    const int base = warp > 0 ? warp_sums[warp - 1] : 0;
+    return base + x - v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_tiles(const int* in, int* out, int n, int* tile_sums)
+{
+    __shared__ int ws[32];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    int ex = block_exclusive_scan(s, ws);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+    if (threadIdx.x == blockDim.x - 1) tile_sums[blockIdx.x] = ex;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_sums(int* tile_sums, int tiles, int* total)
+{
+    __shared__ int ws[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b = 0; b < tiles; b += kScanBlock) {
+        const int k = b + threadIdx.x;
+        const int v = k < tiles ? tile_sums[k] : 0;
+        const int ex = block_exclusive_scan(v, ws);
+        const int c = carry;
+        if (k < tiles) tile_sums[k] = c + ex;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = c + ex + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* out, int n, const int* tile_sums)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] += tile_sums[k / kScanTile];
+}
+
+// exclusive scan of n ints; the sum lands in *total (device)
+cudaError_t exclusive_scan(const int* in, int* out, int n, int* tile_sums, int* total, cudaStream_t s)
+{
+    const int tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles > 0) k_scan_tiles<<<tiles, kScanBlock, 0, s>>>(in, out, n, tile_sums);
+    k_scan_sums<<<1, kScanBlock, 0, s>>>(tile_sums, tiles, total);
+    if (n > 0) k_scan_add<<<(n + 255) / 256, 256, 0, s>>>(out, n, tile_sums);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- energy and adjoint
+
+struct StepArgs {
+    const float2* x;     // positions read
+    float2* y;           // positions written (Adam)
+    float2* gcov;        // coverage gradient (atomics), zeroed by the node pass
+    float2* gout;        // gradient out (energy/gradient call), or NULL
+    const float2* x0;
+    const int4* seg;
+    const uint2* col;
+    const int* seg_off;
+    const int* samp;
+    const float4* tgt;
+    const int* flags;
+    const int2* nbr;
+    float2* m;
+    float2* v;
+    double* energy;      // [3] when not NULL
+    int S, N, ow, scale;
+    float sig, inv_sig, cov_norm, curv_k, dev_k; // cov_norm = w_cov / (3 Ws Hs); curv_k = w_curv / F; dev_k = w_dev / F
+    float lr, bc1, bc2;  // Adam step and bias corrections 1 - beta^t
+    int update;
+};
+
+constexpr float kBeta1 = 0.9f, kBeta2 = 0.999f, kEps = 1e-8f;
+constexpr float kInvSqrt2Pi = 0.3989422804014327f;
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// One warp per segment: Chaikin ends from the nodes, every assigned sample's
+// soft colour, loss and d loss / d ends, reduced and pushed to the nodes.
+__global__ void __launch_bounds__(256) k_rf_coverage(StepArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    float eloss = 0.f;
+    for (int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < a.S; s += warps) {
+        const int4 sg = a.seg[s];
+        const int b0 = a.seg_off[s], b1 = a.seg_off[s + 1];
+        if (sg.w == SEG_NONE || b0 == b1) continue;
+        const int nodes[3] = {sg.x, sg.y, sg.z};
+        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (nodes[k] < 0) continue;
+            const float2 p = a.x[nodes[k]];
+            const float wa = 0.25f * c_seg_wa[sg.w][k], wb = 0.25f * c_seg_wb[sg.w][k];
+            A.x += wa * p.x;
+            A.y += wa * p.y;
+            B.x += wb * p.x;
+            B.y += wb * p.y;
+        }
+        const uint2 c = a.col[s];
+        const float dl[3] = {(float)(int)(c.x & 0xFF) - (float)(int)(c.y & 0xFF),
+                             (float)(int)((c.x >> 8) & 0xFF) - (float)(int)((c.y >> 8) & 0xFF),
+                             (float)(int)((c.x >> 16) & 0xFF) - (float)(int)((c.y >> 16) & 0xFF)};
+        const float cr[3] = {(float)(c.y & 0xFF), (float)((c.y >> 8) & 0xFF), (float)((c.y >> 16) & 0xFF)};
+        const float ex = B.x - A.x, ey = B.y - A.y;
+        const float L2 = ex * ex + ey * ey, L = sqrtf(L2), invL = 1.f / L;
+        float gax = 0.f, gay = 0.f, gbx = 0.f, gby = 0.f;
+        for (int m = b0 + lane; m < b1; m += 32) {
+            const int xs = a.samp[m];
+            const float X = ((xs % a.ow) + 0.5f) / a.scale, Y = ((xs / a.ow) + 0.5f) / a.scale;
+            const float wx = X - A.x, wy = Y - A.y;
+            const float d = (ex * wy - ey * wx) * invL;
+            const float z = d * a.inv_sig;
+            const float Phi = normcdff(z);
+            const float4 t = a.tgt[m];
+            const float r0 = (cr[0] + dl[0] * Phi - t.x) * (1.f / 255.f);
+            const float r1 = (cr[1] + dl[1] * Phi - t.y) * (1.f / 255.f);
+            const float r2 = (cr[2] + dl[2] * Phi - t.z) * (1.f / 255.f);
+            eloss += r0 * r0 + r1 * r1 + r2 * r2;
+            const float phi = expf(-0.5f * z * z) * kInvSqrt2Pi * a.inv_sig;
+            const float dEdd = 2.f * a.cov_norm * (1.f / 255.f) * (r0 * dl[0] + r1 * dl[1] + r2 * dl[2]) * phi;
+            // d d / d e = (wy, -wx) / L - d e / L^2 ; d d / d w = (-ey, ex) / L
+            const float dex = wy * invL - d * ex * invL * invL, dey = -wx * invL - d * ey * invL * invL;
+            const float dwx = -ey * invL, dwy = ex * invL;
+            gbx += dEdd * dex;
+            gby += dEdd * dey;
+            gax += dEdd * (-dex - dwx);
+            gay += dEdd * (-dey - dwy);
+        }
+        gax = warp_sum(gax);
+        gay = warp_sum(gay);
+        gbx = warp_sum(gbx);
+        gby = warp_sum(gby);
+        if (lane < 3 && nodes[lane] >= 0 && !(a.flags[nodes[lane]] & 1)) {
+            const float wa = 0.25f * c_seg_wa[sg.w][lane], wb = 0.25f * c_seg_wb[sg.w][lane];
+            atomicAdd(&a.gcov[nodes[lane]].x, wa * gax + wb * gbx);
+            atomicAdd(&a.gcov[nodes[lane]].y, wa * gay + wb * gby);
+        }
+    }
+    if (a.energy) {
+        eloss = warp_sum(eloss);
+        if (lane == 0 && eloss != 0.f) atomicAdd(&a.energy[2], (double)eloss * (double)a.cov_norm);
+    }
+}
+
+// One thread per node: curvature and deviation gradients (gathered from the
+// node's own and its free neighbours' second differences), the coverage
+// gradient, then an Adam step (or the gradient written out).
+__global__ void __launch_bounds__(256) k_rf_nodes_step(StepArgs a)
+{
+    float ec = 0.f, ed = 0.f;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.N; k += gridDim.x * blockDim.x) {
+        if (a.flags[k] & 1) {
+            if (a.gout) a.gout[k] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float2 p = a.x[k];
+        const int2 nb = a.nbr[k];
+        const float2 pa = a.x[nb.x], pb = a.x[nb.y];
+        const float tx = pa.x - 2.f * p.x + pb.x, ty = pa.y - 2.f * p.y + pb.y;
+        float gx = -2.f * tx, gy = -2.f * ty;
+        const int q2[2] = {nb.x, nb.y};
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            const int q = q2[s];
+            if (a.flags[q] & 1) continue;
+            const int2 qn = a.nbr[q];
+            const float2 qa = a.x[qn.x], qq = a.x[q], qb = a.x[qn.y];
+            gx += qa.x - 2.f * qq.x + qb.x;
+            gy += qa.y - 2.f * qq.y + qb.y;
+        }
+        const float2 p0 = a.x0[k];
+        const float dx = p.x - p0.x, dy = p.y - p0.y;
+        const float2 gc = a.gcov[k];
+        gx = 0.25f * a.curv_k * gx + 2.f * a.dev_k * dx + gc.x;
+        gy = 0.25f * a.curv_k * gy + 2.f * a.dev_k * dy + gc.y;
+        a.gcov[k] = make_float2(0.f, 0.f);
+        if (a.energy) {
+            ec += 0.125f * (tx * tx + ty * ty);
+            ed += dx * dx + dy * dy;
+        }
+        if (a.gout) a.gout[k] = make_float2(gx, gy);
+        if (a.update) {
+            float2 m = a.m[k], v = a.v[k];
+            m.x = kBeta1 * m.x + (1.f - kBeta1) * gx;
+            m.y = kBeta1 * m.y + (1.f - kBeta1) * gy;
+            v.x = kBeta2 * v.x + (1.f - kBeta2) * gx * gx;
+            v.y = kBeta2 * v.y + (1.f - kBeta2) * gy * gy;
+            a.m[k] = m;
+            a.v[k] = v;
+            a.y[k] = make_float2(p.x - a.lr * (m.x / a.bc1) / (sqrtf(v.x / a.bc2) + kEps),
+                                 p.y - a.lr * (m.y / a.bc1) / (sqrtf(v.y / a.bc2) + kEps));
+        }
+    }
+    if (a.energy) {
+        ec = warp_sum(ec);
+        ed = warp_sum(ed);
+        if ((threadIdx.x & 31) == 0) {
+            if (ec != 0.f) atomicAdd(&a.energy[0], (double)ec * (double)a.curv_k);
+            if (ed != 0.f) atomicAdd(&a.energy[1], (double)ed * (double)a.dev_k);
+        }
+    }
+}
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n)
+    {
+        if (n <= cap && p) return cudaSuccess;
+        cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+    void release()
+    {
+        cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+}  // namespace depix
+
+using namespace depix;
+
+struct depix_refiner {
+    int device = 0;
+    size_t max_pixels = 0;
+    int sms = 0;
+    const uint64_t* lut = nullptr;
+    // frame
+    int w = 0, h = 0, scale = 0, ow = 0, oh = 0;
+    int E = 0, N = 0, F = 0, S = 0, M = 0;
+    float sigma = 0.5f; // coverage sigma of the targets (output pixels)
+    DevBuf<uint32_t> vgrid;
+    DevBuf<int> cell_count, cell_off, is_node, nid, tile_sums, scalars;
+    DevBuf<int2> nb_v, nb_e;
+    DevBuf<int4> edges;
+    DevBuf<int2> node_q, node_nbr, node_nbr_edge;
+    DevBuf<int> node_flags;
+    DevBuf<float2> pos0, pos_a, pos_b, gcov, adam_m, adam_v;
+    DevBuf<int4> seg;
+    DevBuf<uint2> seg_col;
+    DevBuf<unsigned long long> best;
+    DevBuf<int> bseg, seg_count, seg_off, cursor, samp;
+    DevBuf<float4> tgt;
+    DevBuf<double> energy;
+    int* h_scalars = nullptr; // pinned
+    double* h_energy = nullptr;
+    bool ready = false;
+};
+
+namespace {
+
+depix_status rf_fail(cudaError_t e, const char* where)
+{
+    set_last_error(std::string(where) + ": " + cudaGetErrorString(e));
+    return DEPIX_ERR_CUDA;
+}
+
+#define DEPIX_TRY_RF(call)                                              \
+    do {                                                                \
+        depix_status st_ = (call);                                      \
+        if (st_ != DEPIX_OK) return st_;                                \
+    } while (0)
+
+#define RF_CK(call)                                                     \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return rf_fail(e_, #call);               \
+    } while (0)
+
+int blocks_for(long long n, int t = 256) { return (int)std::max<long long>(1, (n + t - 1) / t); }
+
+// total of the last exclusive scan, read back to the host (synchronous)
+depix_status read_total(depix_refiner* r, int slot, int* out, cudaStream_t s)
+{
+    RF_CK(cudaMemcpyAsync(r->h_scalars + slot, r->scalars.p + slot, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RF_CK(cudaStreamSynchronize(s));
+    *out = r->h_scalars[slot];
+    return DEPIX_OK;
+}
+
+depix_status check_refiner(depix_refiner* r)
+{
+    if (!r) {
+        set_last_error("NULL refiner");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    if (!r->ready) {
+        set_last_error("refiner has no frame: call depix_refine_setup first");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    return DEPIX_OK;
+}
+
+StepArgs step_args(depix_refiner* r, const depix_refine_params* p)
+{
+    StepArgs a{};
+    a.gcov = r->gcov.p;
+    a.x0 = r->pos0.p;
+    a.seg = r->seg.p;
+    a.col = r->seg_col.p;
+    a.seg_off = r->seg_off.p;
+    a.samp = r->samp.p;
+    a.tgt = r->tgt.p;
+    a.flags = r->node_flags.p;
+    a.nbr = r->node_nbr.p;
+    a.m = r->adam_m.p;
+    a.v = r->adam_v.p;
+    a.S = r->S;
+    a.N = r->N;
+    a.ow = r->ow;
+    a.scale = r->scale;
+    a.sig = r->sigma / (float)r->scale;
+    a.inv_sig = 1.f / a.sig;
+    a.cov_norm = (float)((double)p->w_coverage / (3.0 * (double)r->ow * (double)r->oh));
+    const float F = (float)std::max(r->F, 1);
+    a.curv_k = p->w_curvature / F;
+    a.dev_k = p->w_deviation / F;
+    a.lr = p->lr;
+    return a;
+}
+
+depix_status check_rparams(const depix_refine_params* p)
+{
+    if (!p || !(p->sigma > 0.f) || !(p->lr >= 0.f) || p->steps < 0 || !(p->w_curvature >= 0.f) ||
+        !(p->w_deviation >= 0.f) || !(p->w_coverage >= 0.f)) {
+        set_last_error("refine params: sigma > 0, lr, weights >= 0, steps >= 0");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    return DEPIX_OK;
+}
+
+depix_status check_sigma(const depix_refiner* r, const depix_refine_params* p)
+{
+    if (p->sigma != r->sigma) {
+        set_last_error("coverage sigma differs from the one the targets were set up with");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    return DEPIX_OK;
+}
+
+int cov_blocks(const depix_refiner* r) { return std::max(1, std::min(r->sms * 8, blocks_for((long long)r->S * 32))); }
+int node_blocks(const depix_refiner* r) { return std::max(1, std::min(r->sms * 8, blocks_for(r->N))); }
+
+// energy (and gradient when gout) at positions x, without an update
+depix_status eval(depix_refiner* r, const depix_refine_params* p, const float2* x, float2* gout, double out[4],
+                  cudaStream_t s)
+{
+    StepArgs a = step_args(r, p);
+    a.x = x;
+    a.gout = gout;
+    a.energy = r->energy.p;
+    a.update = 0;
+    RF_CK(cudaMemsetAsync(r->energy.p, 0, 3 * sizeof(double), s));
+    k_rf_coverage<<<cov_blocks(r), 256, 0, s>>>(a);
+    k_rf_nodes_step<<<node_blocks(r), 256, 0, s>>>(a);
+    RF_CK(cudaGetLastError());
+    RF_CK(cudaMemcpyAsync(r->h_energy, r->energy.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RF_CK(cudaStreamSynchronize(s));
+    out[0] = r->h_energy[0];
+    out[1] = r->h_energy[1];
+    out[2] = r->h_energy[2];
+    out[3] = out[0] + out[1] + out[2];
+    return DEPIX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void depix_refine_default_params(depix_refine_params* p)
+{
+    if (!p) return;
+    p->w_curvature = 1.0f;
+    p->w_deviation = 0.25f;
+    p->w_coverage = 1.0f;
+    p->sigma = 0.5f;
+    p->lr = 0.05f;
+    p->steps = 200;
+}
+
+depix_status depix_refiner_create(depix_refiner** out, size_t max_pixels)
+{
+    if (!out) {
+        set_last_error("NULL refiner pointer");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (max_pixels < 1) {
+        set_last_error("capacity must be >= 1");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    depix_status st = depix_init_device();
+    if (st != DEPIX_OK) return st;
+    depix_refiner* r = new (std::nothrow) depix_refiner();
+    if (!r) return DEPIX_ERR_ALLOC;
+    r->max_pixels = max_pixels;
+    cudaError_t e = cudaGetDevice(&r->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, r->device);
+    if (e == cudaSuccess) e = hull_table_address(&r->lut);
+    if (e == cudaSuccess) e = r->scalars.reserve(8);
+    if (e == cudaSuccess) e = r->energy.reserve(3);
+    if (e == cudaSuccess) e = cudaHostAlloc(&r->h_scalars, 8 * sizeof(int), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&r->h_energy, 4 * sizeof(double), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        depix_refiner_destroy(r);
+        set_last_error(std::string("refiner set-up: ") + cudaGetErrorString(e));
+        return DEPIX_ERR_ALLOC;
+    }
+    *out = r;
+    return DEPIX_OK;
+}
+
+depix_status depix_refiner_destroy(depix_refiner* r)
+{
+    if (!r) return DEPIX_OK;
+    r->vgrid.release();
+    r->cell_count.release(); r->cell_off.release(); r->is_node.release(); r->nid.release();
+    r->tile_sums.release(); r->scalars.release();
+    r->nb_v.release(); r->nb_e.release(); r->edges.release();
+    r->node_q.release(); r->node_nbr.release(); r->node_nbr_edge.release(); r->node_flags.release();
+    r->pos0.release(); r->pos_a.release(); r->pos_b.release(); r->gcov.release();
+    r->adam_m.release(); r->adam_v.release();
+    r->seg.release(); r->seg_col.release(); r->best.release(); r->bseg.release();
+    r->seg_count.release(); r->seg_off.release(); r->cursor.release(); r->samp.release(); r->tgt.release();
+    r->energy.release();
+    cudaFreeHost(r->h_scalars);
+    cudaFreeHost(r->h_energy);
+    delete r;
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, int h, int widthstep,
+                                depix_layout layout, const uint8_t* d_graph, const depix_params* p,
+                                const depix_refine_params* rp, depix_stream s_)
+{
+    DEPIX_TRY_RF(check_rparams(rp));
+    if (!r || !d_img || !d_graph || !p || w < 1 || h < 1) {
+        set_last_error("refine setup: NULL argument or size below 1");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    if ((size_t)w * h > r->max_pixels) {
+        set_last_error("frame larger than the refiner capacity");
+        return DEPIX_ERR_TOO_LARGE;
+    }
+    if (p->scale < 1 || p->scale > kMaxRefineScale) {
+        set_last_error("refine scale must be in 1..12");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    if (layout == DEPIX_LAYOUT_RGBA ? (widthstep < 4 * w || (widthstep & 3)) : (layout != DEPIX_LAYOUT_BGR || widthstep < 3 * w)) {
+        set_last_error("refine setup: bad layout or widthstep");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(s_);
+    r->ready = false;
+    const int n = w * h, gw = 4 * w + 3, gh = 4 * h + 3, nv = gw * gh;
+    Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, pack_thresholds(p->tr_y, p->tr_u, p->tr_v)};
+    RF_CK(r->vgrid.reserve(nv));
+    RF_CK(r->cell_count.reserve(n));
+    RF_CK(r->cell_off.reserve(n));
+    RF_CK(r->is_node.reserve(nv));
+    RF_CK(r->nid.reserve(nv));
+    RF_CK(r->nb_v.reserve(nv));
+    RF_CK(r->nb_e.reserve(nv));
+    RF_CK(r->tile_sums.reserve((size_t)nv / kScanTile + 2));
+    RF_CK(cudaMemsetAsync(r->vgrid.p, 0, (size_t)nv * sizeof(uint32_t), s));
+    k_rf_mark_vertices<<<blocks_for(n), 256, 0, s>>>(G, r->vgrid.p);
+    k_rf_count_edges<<<blocks_for(n, 128), 128, 0, s>>>(G, r->vgrid.p, r->cell_count.p);
+    RF_CK(cudaGetLastError());
+    RF_CK(exclusive_scan(r->cell_count.p, r->cell_off.p, n, r->tile_sums.p, r->scalars.p + 0, s));
+    int E = 0;
+    DEPIX_TRY_RF(read_total(r, 0, &E, s));
+    RF_CK(r->edges.reserve(E));
+    k_rf_emit_edges<<<blocks_for(n, 128), 128, 0, s>>>(G, r->vgrid.p, r->cell_off.p, r->edges.p, r->nb_v.p, r->nb_e.p);
+    k_rf_node_flags<<<blocks_for(nv), 256, 0, s>>>(r->vgrid.p, nv, r->is_node.p);
+    RF_CK(cudaGetLastError());
+    RF_CK(exclusive_scan(r->is_node.p, r->nid.p, nv, r->tile_sums.p, r->scalars.p + 1, s));
+    int N = 0;
+    DEPIX_TRY_RF(read_total(r, 1, &N, s));
+    RF_CK(r->node_q.reserve(N));
+    RF_CK(r->node_flags.reserve(N));
+    RF_CK(r->node_nbr.reserve(N));
+    RF_CK(r->node_nbr_edge.reserve(N));
+    RF_CK(r->pos0.reserve(N));
+    RF_CK(r->pos_a.reserve(N));
+    RF_CK(r->pos_b.reserve(N));
+    RF_CK(r->gcov.reserve(N));
+    RF_CK(r->adam_m.reserve(N));
+    RF_CK(r->adam_v.reserve(N));
+    NodeOut no{r->node_q.p, r->node_flags.p, r->node_nbr.p, r->node_nbr_edge.p, r->pos0.p};
+    k_rf_nodes<<<blocks_for(nv), 256, 0, s>>>(G, r->vgrid.p, r->nid.p, r->nb_v.p, r->nb_e.p, no);
+    RF_CK(cudaGetLastError());
+    const int S = 3 * E + N;
+    RF_CK(r->seg.reserve(S));
+    RF_CK(r->seg_col.reserve(S));
+    k_rf_segments<<<blocks_for((long long)E + N), 256, 0, s>>>(G, r->nid.p, r->edges.p, E, N, r->node_flags.p,
+                                                              r->node_nbr.p, r->node_nbr_edge.p,
+                                                              SegOut{r->seg.p, r->seg_col.p});
+    // sample assignment
+    const int ow = w * p->scale, oh = h * p->scale, no_px = ow * oh;
+    RF_CK(r->best.reserve(no_px));
+    RF_CK(r->bseg.reserve(no_px));
+    RF_CK(r->seg_count.reserve((size_t)S + 1));
+    RF_CK(r->seg_off.reserve((size_t)S + 1));
+    RF_CK(r->cursor.reserve((size_t)S + 1));
+    RF_CK(r->tile_sums.reserve((size_t)std::max(nv, S + 1) / kScanTile + 2));
+    RF_CK(cudaMemsetAsync(r->best.p, 0xFF, (size_t)no_px * sizeof(unsigned long long), s));
+    RF_CK(cudaMemsetAsync(r->bseg.p, 0x7F, (size_t)no_px * sizeof(int), s)); // kNoSeg
+    k_rf_assign_dist<<<blocks_for(S, 128), 128, 0, s>>>(r->seg.p, S, r->node_q.p, p->scale, ow, oh, r->best.p);
+    k_rf_assign_seg<<<blocks_for(S, 128), 128, 0, s>>>(r->seg.p, S, r->node_q.p, p->scale, ow, oh, r->best.p,
+                                                       r->bseg.p);
+    RF_CK(cudaMemsetAsync(r->seg_count.p, 0, ((size_t)S + 1) * sizeof(int), s));
+    k_rf_count_samples<<<blocks_for(no_px), 256, 0, s>>>(r->bseg.p, no_px, r->seg_count.p);
+    RF_CK(cudaGetLastError());
+    RF_CK(exclusive_scan(r->seg_count.p, r->seg_off.p, S + 1, r->tile_sums.p, r->scalars.p + 2, s));
+    int M = 0;
+    DEPIX_TRY_RF(read_total(r, 2, &M, s));
+    RF_CK(r->samp.reserve(M));
+    RF_CK(r->tgt.reserve(M));
+    RF_CK(cudaMemsetAsync(r->cursor.p, 0, ((size_t)S + 1) * sizeof(int), s));
+    k_rf_scatter_samples<<<blocks_for(no_px), 256, 0, s>>>(r->bseg.p, no_px, r->seg_off.p, r->cursor.p, r->samp.p);
+    k_rf_sort_samples<<<blocks_for(S), 256, 0, s>>>(r->seg_off.p, S, r->samp.p);
+    k_rf_targets<<<blocks_for(M), 256, 0, s>>>(G, p->scale, (double)rp->sigma / p->scale, r->samp.p, M, r->tgt.p);
+    RF_CK(cudaGetLastError());
+    // free nodes
+    RF_CK(cudaMemsetAsync(r->scalars.p + 3, 0, sizeof(int), s));
+    k_rf_count_free<<<blocks_for(N), 256, 0, s>>>(r->node_flags.p, N, r->scalars.p + 3);
+    RF_CK(cudaMemsetAsync(r->gcov.p, 0, (size_t)std::max(N, 1) * sizeof(float2), s));
+    int F = 0;
+    DEPIX_TRY_RF(read_total(r, 3, &F, s));
+    r->w = w;
+    r->h = h;
+    r->scale = p->scale;
+    r->ow = ow;
+    r->oh = oh;
+    r->E = E;
+    r->N = N;
+    r->F = F;
+    r->S = S;
+    r->M = M;
+    r->sigma = rp->sigma;
+    r->ready = true;
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_counts(depix_refiner* r, long long counts[5])
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    if (!counts) {
+        set_last_error("NULL counts");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    counts[0] = r->N;
+    counts[1] = r->F;
+    counts[2] = r->E;
+    counts[3] = r->S;
+    counts[4] = r->M;
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_export(depix_refiner* r, int32_t* node_q, int32_t* node_flags, int32_t* node_nbr,
+                                 int32_t* edges, int32_t* segs, uint32_t* seg_colors, int32_t* samples)
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    RF_CK(cudaDeviceSynchronize());
+    if (node_q) RF_CK(cudaMemcpy(node_q, r->node_q.p, (size_t)r->N * sizeof(int2), cudaMemcpyDeviceToHost));
+    if (node_flags) RF_CK(cudaMemcpy(node_flags, r->node_flags.p, (size_t)r->N * sizeof(int), cudaMemcpyDeviceToHost));
+    if (node_nbr) RF_CK(cudaMemcpy(node_nbr, r->node_nbr.p, (size_t)r->N * sizeof(int2), cudaMemcpyDeviceToHost));
+    if (edges) {
+        // vertex indices -> node ids on the host copy
+        std::vector<int4> ev(r->E);
+        std::vector<int> nid((size_t)(4 * r->w + 3) * (4 * r->h + 3));
+        RF_CK(cudaMemcpy(ev.data(), r->edges.p, (size_t)r->E * sizeof(int4), cudaMemcpyDeviceToHost));
+        RF_CK(cudaMemcpy(nid.data(), r->nid.p, nid.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int e = 0; e < r->E; e++) {
+            edges[4 * e] = nid[ev[e].x];
+            edges[4 * e + 1] = nid[ev[e].y];
+            edges[4 * e + 2] = ev[e].z;
+            edges[4 * e + 3] = ev[e].w;
+        }
+    }
+    if (segs) RF_CK(cudaMemcpy(segs, r->seg.p, (size_t)r->S * sizeof(int4), cudaMemcpyDeviceToHost));
+    if (seg_colors) RF_CK(cudaMemcpy(seg_colors, r->seg_col.p, (size_t)r->S * sizeof(uint2), cudaMemcpyDeviceToHost));
+    if (samples) {
+        std::vector<int> off((size_t)r->S + 1), smp(r->M);
+        RF_CK(cudaMemcpy(off.data(), r->seg_off.p, off.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        RF_CK(cudaMemcpy(smp.data(), r->samp.p, smp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int sg = 0; sg < r->S; sg++)
+            for (int m = off[sg]; m < off[sg + 1]; m++) {
+                samples[2 * m] = smp[m];
+                samples[2 * m + 1] = sg;
+            }
+    }
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_initial(depix_refiner* r, float* d_pos, depix_stream s)
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    if (!d_pos) {
+        set_last_error("NULL positions");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    RF_CK(cudaMemcpyAsync(d_pos, r->pos0.p, (size_t)r->N * sizeof(float2), cudaMemcpyDeviceToDevice,
+                          reinterpret_cast<cudaStream_t>(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_energy_grad(depix_refiner* r, const depix_refine_params* p, const float* d_pos,
+                                      float* d_grad, double energy[4], depix_stream s)
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    DEPIX_TRY_RF(check_rparams(p));
+    DEPIX_TRY_RF(check_sigma(r, p));
+    if (!d_pos || !energy) {
+        set_last_error("NULL positions or energy");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    return eval(r, p, reinterpret_cast<const float2*>(d_pos), reinterpret_cast<float2*>(d_grad), energy,
+                reinterpret_cast<cudaStream_t>(s));
+}
+
+depix_status depix_refine_run(depix_refiner* r, const depix_refine_params* p, float* d_pos, double before[4],
+                              double after[4], depix_stream s_)
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    DEPIX_TRY_RF(check_rparams(p));
+    DEPIX_TRY_RF(check_sigma(r, p));
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(s_);
+    const size_t bytes = (size_t)r->N * sizeof(float2);
+    float2* x = r->pos_a.p;
+    float2* y = r->pos_b.p;
+    RF_CK(cudaMemcpyAsync(x, d_pos ? reinterpret_cast<const float2*>(d_pos) : r->pos0.p, bytes,
+                          cudaMemcpyDeviceToDevice, s));
+    // pinned nodes never move: both buffers start equal
+    RF_CK(cudaMemcpyAsync(y, x, bytes, cudaMemcpyDeviceToDevice, s));
+    RF_CK(cudaMemsetAsync(r->adam_m.p, 0, bytes, s));
+    RF_CK(cudaMemsetAsync(r->adam_v.p, 0, bytes, s));
+    if (before) DEPIX_TRY_RF(eval(r, p, x, nullptr, before, s));
+    StepArgs a = step_args(r, p);
+    a.update = 1;
+    const int cb = cov_blocks(r), nb = node_blocks(r);
+    double b1 = 1.0, b2 = 1.0;
+    for (int t = 1; t <= p->steps; t++) {
+        b1 *= (double)kBeta1;
+        b2 *= (double)kBeta2;
+        a.x = x;
+        a.y = y;
+        a.bc1 = (float)(1.0 - b1);
+        a.bc2 = (float)(1.0 - b2);
+        k_rf_coverage<<<cb, 256, 0, s>>>(a);
+        k_rf_nodes_step<<<nb, 256, 0, s>>>(a);
+        std::swap(x, y);
+    }
+    RF_CK(cudaGetLastError());
+    if (after) DEPIX_TRY_RF(eval(r, p, x, nullptr, after, s));
+    if (d_pos) RF_CK(cudaMemcpyAsync(d_pos, x, bytes, cudaMemcpyDeviceToDevice, s));
+    return DEPIX_OK;
+}
+
+}  // extern "C"

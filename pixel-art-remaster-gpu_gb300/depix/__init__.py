@@ -29,6 +29,15 @@ class Params(ctypes.Structure):
                 ("subdivide", ctypes.c_int), ("scale", ctypes.c_int)]
 
 
+class RefineParams(ctypes.Structure):
+    _fields_ = [("w_curvature", ctypes.c_float), ("w_deviation", ctypes.c_float), ("w_coverage", ctypes.c_float),
+                ("sigma", ctypes.c_float), ("lr", ctypes.c_float), ("steps", ctypes.c_int)]
+
+
+def refine_params(w_curvature=1.0, w_deviation=0.25, w_coverage=1.0, sigma=0.5, lr=0.05, steps=200):
+    return RefineParams(w_curvature, w_deviation, w_coverage, sigma, lr, steps)
+
+
 def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4) -> Params:
     return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale)
 
@@ -77,6 +86,16 @@ def lib():
         _sig(L, "depix_context_stage_times", [_vp, _vp, _vp, _vp])
         _sig(L, "depix_launch_kernel_compat", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, _i, P], _vp)
         _sig(L, "launch_kernel", [_vp, _vp, ctypes.c_float, _vp, _i, _i, _i, _vp, _vp, ctypes.c_bool], _vp)
+        RP = ctypes.POINTER(RefineParams)
+        _sig(L, "depix_refine_default_params", [RP], None)
+        _sig(L, "depix_refiner_create", [ctypes.POINTER(_vp), ctypes.c_size_t])
+        _sig(L, "depix_refiner_destroy", [_vp])
+        _sig(L, "depix_refine_setup", [_vp, _vp, _i, _i, _i, _i, _vp, P, RP, _vp])
+        _sig(L, "depix_refine_counts", [_vp, _vp])
+        _sig(L, "depix_refine_export", [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_refine_initial", [_vp, _vp, _vp])
+        _sig(L, "depix_refine_energy_grad", [_vp, RP, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_refine_run", [_vp, RP, _vp, _vp, _vp, _vp])
         _sig(L, "depix_yuv_words", [_vp, ctypes.c_size_t, _vp, _vp])
         _sig(L, "depix_pattern_tables", [_vp, _vp])
         _lib = L
@@ -233,6 +252,65 @@ class Context:
         ca = (ctypes.c_longlong * 4)()
         _check(lib().depix_context_stage_times(self.handle, ms, la, ca), "depix_context_stage_times")
         return {name: (ms[k], la[k], ca[k]) for k, name in enumerate(self.STAGES)}
+
+
+class Refiner:
+    """Spline refinement of one frame at a time (topology frozen at setup)."""
+
+    def __init__(self, max_pixels):
+        h = _vp()
+        _check(lib().depix_refiner_create(ctypes.byref(h), max_pixels), "depix_refiner_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().depix_refiner_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup(self, img, w, h, ws, layout, graph, p, rp, stream=None):
+        _check(lib().depix_refine_setup(self.handle, ptr(img), w, h, ws, layout, ptr(graph), ctypes.byref(p),
+                                        ctypes.byref(rp), stream_ptr(stream)), "depix_refine_setup")
+
+    def counts(self):
+        """dict of nodes, free, edges, segments (slots), samples."""
+        c = (ctypes.c_longlong * 5)()
+        _check(lib().depix_refine_counts(self.handle, c), "depix_refine_counts")
+        return dict(zip(("nodes", "free", "edges", "segments", "samples"), list(c)))
+
+    def export(self):
+        import numpy as np
+        c = self.counts()
+        N, E, S, M = c["nodes"], c["edges"], c["segments"], c["samples"]
+        out = dict(q=np.zeros((N, 2), np.int32), flags=np.zeros(N, np.int32), nbr=np.zeros((N, 2), np.int32),
+                   edges=np.zeros((E, 4), np.int32), segs=np.zeros((S, 4), np.int32),
+                   cols=np.zeros((S, 2), np.uint32), samples=np.zeros((M, 2), np.int32))
+        _check(lib().depix_refine_export(self.handle, *(ptr(out[k]) for k in
+                                                        ("q", "flags", "nbr", "edges", "segs", "cols", "samples"))),
+               "depix_refine_export")
+        return out
+
+    def initial(self, pos, stream=None):
+        _check(lib().depix_refine_initial(self.handle, ptr(pos), stream_ptr(stream)), "depix_refine_initial")
+
+    def energy_grad(self, rp, pos, grad=None, stream=None):
+        e = (ctypes.c_double * 4)()
+        _check(lib().depix_refine_energy_grad(self.handle, ctypes.byref(rp), ptr(pos), ptr(grad), e,
+                                              stream_ptr(stream)), "depix_refine_energy_grad")
+        return tuple(e)
+
+    def run(self, rp, pos=None, stream=None):
+        """Adam; returns (energy before, energy after) as 4-tuples."""
+        b = (ctypes.c_double * 4)()
+        a = (ctypes.c_double * 4)()
+        _check(lib().depix_refine_run(self.handle, ctypes.byref(rp), ptr(pos), b, a, stream_ptr(stream)),
+               "depix_refine_run")
+        return tuple(b), tuple(a)
 
 
 def launch_kernel_compat(pos, col, img_host, w, h, ws, edge_count_host, graph_host, subdivide, p=None):
