@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sprites", type=int, default=4096, help="sprites in the uneven-batch leg")
     ap.add_argument("--no-sprites", action="store_true")
+    ap.add_argument("--no-refine", action="store_true")
     return ap.parse_args()
 
 
@@ -291,6 +292,7 @@ def run_ours(args, rank, world, local_rank):
     ctx1.close()
 
     sprites = None if args.no_sprites else run_sprites(args, dev, stream)
+    refine = None if args.no_refine else run_refine(args, dev, stream, cpu=(rank == 0 and world == 1 and not args.no_cpu))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -307,7 +309,8 @@ def run_ours(args, rank, world, local_rank):
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
-                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites}
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
+                "refine": refine}
         print(json.dumps(line))
 
 
@@ -392,6 +395,75 @@ def run_sprites(args, dev, stream):
             "stage_ms_per_batch": {k: round(v[0] / max(v[2], 1), 4) for k, v in st.items()},
             "launch_shape": {"gran": list(gran), "raster_tile": [tw, th]}, "first_call_s": round(tune_s, 3),
             "plain_frames_per_s": round(n / (plain_ms / 1e3), 1), "plain_host_wall_s": round(plain_wall, 3)}
+
+
+def run_refine(args, dev, stream, cpu):
+    """Spline refinement of the 256x224 frame: topology setup, then 200 Adam
+    steps of the curvature + deviation + soft-coverage energy (x4, sigma 0.5
+    output px) through the adjoint kernel; steps/s, ms per frame, energy cut;
+    the float64 CPU specification timed on a few steps beside it."""
+    import numpy as np
+    import torch
+    import depix
+
+    img = make_frames(1)[0]
+    d_img = torch.from_numpy(np.ascontiguousarray(img).reshape(-1)).to(dev)
+    ctx = depix.Context(W * H, 1)
+    p = depix.params(48, 7, 6, True, SCALE)
+    d_graph = torch.empty(W * H, dtype=torch.uint8, device=dev)
+    ctx.frame(d_img, W, H, 4 * W, depix.LAYOUT_RGBA, p, None, d_graph, None, stream=stream)
+    rp = depix.refine_params()
+    rf = depix.Refiner(W * H)
+    rf.setup(d_img, W, H, 4 * W, depix.LAYOUT_RGBA, d_graph, p, rp, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        rf.setup(d_img, W, H, 4 * W, depix.LAYOUT_RGBA, d_graph, p, rp, stream=stream)
+    torch.cuda.synchronize()
+    setup_ms = (time.perf_counter() - t0) / reps * 1e3
+    c = rf.counts()
+    pos = torch.empty(2 * max(c["nodes"], 1), dtype=torch.float32, device=dev)
+    rf.initial(pos, stream=stream)
+    before, after = rf.run(rp, pos, stream=stream)
+    for _ in range(2):
+        rf.run(rp, None, stream=stream, energies=False)
+    torch.cuda.synchronize()
+    runs = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(runs):
+        rf.run(rp, None, stream=stream, energies=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / runs
+    out = {"workload": f"256x224 frame (seeded generator), x4 coverage, {c['nodes']} nodes ({c['free']} free), "
+                       f"{c['edges']} curve edges, {c['samples']} samples, {rp.steps} Adam steps",
+           "steps_per_s": round(rp.steps / (ms / 1e3), 1), "ms_per_frame": round(ms, 3),
+           "setup_ms": round(setup_ms, 3), "energy_before": round(before[3], 6), "energy_after": round(after[3], 6),
+           "energy_cut": round(1 - after[3] / before[3], 4),
+           "terms_after": {"curvature": round(after[0], 6), "deviation": round(after[1], 6),
+                           "coverage": round(after[2], 6)}}
+    rf.close()
+    ctx.close()
+    if cpu:
+        sys.path.insert(0, ORACLE)
+        import oracle as O
+        import refine_oracle as R
+        from depix import synth
+        bgr, ws = synth.rgba_to_bgr(img)
+        raw, _, res = O.graph(bgr, W, H, ws, (48, 7, 6))
+        top = R.topology(img, res, raw, SCALE)
+        k = 5
+        P0 = R.initial_positions(top)
+        t0 = time.perf_counter()
+        for _ in range(k):  # an Adam step is one energy + gradient evaluation and an update
+            R.energy_grad(top, P0, P0, img)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"steps_per_s": round(k / dt, 2), "cores": 1, "kind": "port",
+                               "sample": f"{k} Adam steps of the float64 numpy specification "
+                                         f"(oracle/refine_oracle.py) on the same frame and topology"}
+    return out
 
 
 # ---------------------------------------------------------- reference arm

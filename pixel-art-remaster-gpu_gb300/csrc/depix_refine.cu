@@ -44,9 +44,17 @@ namespace {
 constexpr int kBand = 48;          // 1.5 output pixels in 1/(32 s) source pixel
 constexpr int kMaxRefineScale = 12;
 enum SegType { SEG_NONE = 0, SEG_MID = 1, SEG_PIN_U = 2, SEG_PIN_V = 3, SEG_CORNER = 4 };
-// weights (x4) of a segment's ends over its three node slots, per type
-__constant__ int8_t c_seg_wa[5][3] = {{0, 0, 0}, {3, 1, 0}, {4, 0, 0}, {1, 3, 0}, {1, 3, 0}};
-__constant__ int8_t c_seg_wb[5][3] = {{0, 0, 0}, {1, 3, 0}, {3, 1, 0}, {0, 4, 0}, {0, 3, 1}};
+// weights (x4) of a segment's ends over its three node slots, per type, as
+// 4-bit fields (type * 12 + slot * 4): A {-, 3 1 0, 4 0 0, 1 3 0, 1 3 0},
+// B {-, 1 3 0, 3 1 0, 0 4 0, 0 3 1}
+constexpr unsigned long long kSegWA = 0x031031004013000ull;
+constexpr unsigned long long kSegWB = 0x130040013031000ull;
+__host__ __device__ constexpr int seg_wa(int type, int k) { return (int)((kSegWA >> (type * 12 + k * 4)) & 0xF); }
+__host__ __device__ constexpr int seg_wb(int type, int k) { return (int)((kSegWB >> (type * 12 + k * 4)) & 0xF); }
+static_assert(seg_wa(1, 0) == 3 && seg_wa(1, 1) == 1 && seg_wa(2, 0) == 4 && seg_wa(3, 1) == 3 && seg_wa(4, 1) == 3,
+              "segment weights A");
+static_assert(seg_wb(1, 1) == 3 && seg_wb(2, 0) == 3 && seg_wb(2, 1) == 1 && seg_wb(3, 1) == 4 && seg_wb(4, 2) == 1 &&
+              seg_wb(4, 1) == 3 && seg_wb(4, 0) == 0, "segment weights B");
 
 // vertex grid word: bit 0 a hull vertex, bit 1 on an edge without a twin,
 // bits 8.. the number of curve edges
@@ -309,10 +317,10 @@ __device__ __forceinline__ void seg_ends(const int4 sg, const int2* q, int scale
     for (int k = 0; k < 3; k++) {
         if (nodes[k] < 0) continue;
         const int2 p = q[nodes[k]];
-        ax += (long long)c_seg_wa[sg.w][k] * p.x;
-        ay += (long long)c_seg_wa[sg.w][k] * p.y;
-        bx += (long long)c_seg_wb[sg.w][k] * p.x;
-        by += (long long)c_seg_wb[sg.w][k] * p.y;
+        ax += (long long)seg_wa(sg.w, k) * p.x;
+        ay += (long long)seg_wa(sg.w, k) * p.y;
+        bx += (long long)seg_wb(sg.w, k) * p.x;
+        by += (long long)seg_wb(sg.w, k) * p.y;
     }
     const long long m = 2 * scale; // weights x4, quarter -> 1/(32 s): x 8 s / 4
     ax *= m;
@@ -388,17 +396,6 @@ __global__ void k_rf_scatter_samples(const int* bseg, int n, const int* seg_off,
     if (x >= n || bseg[x] == kNoSeg) return;
     const int s = bseg[x];
     samp[seg_off[s] + atomicAdd(&cursor[s], 1)] = x;
-}
-
-__global__ void k_rf_count_free(const int* flags, int n, int* out)
-{
-    __shared__ int c;
-    if (threadIdx.x == 0) c = 0;
-    __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n && !(flags[k] & 1)) atomicAdd(&c, 1);
-    __syncthreads();
-    if (threadIdx.x == 0 && c) atomicAdd(out, c);
 }
 
 // each segment's samples in ascending order (summation order fixed)
@@ -530,6 +527,32 @@ cudaError_t exclusive_scan(const int* in, int* out, int n, int* tile_sums, int* 
 
 // ------------------------------------------------------- energy and adjoint
 
+// Frame sizes the step kernels read from device memory, so that a captured
+// graph of the Adam loop serves every frame of the same buffers.
+struct RefineFrame {
+    int N;      // nodes
+    int L;      // live segments (with samples)
+    int ow, oh; // output raster
+    int scale;
+    int F;      // free nodes
+    float inv_samples3; // 1 / (3 ow oh), rounded once on the host
+};
+
+// A live segment, packed for one load: its nodes and type, its sample
+// range and its colours.
+struct LiveSeg {
+    int4 nodes;  // n0, n1, n2, type
+    int4 range;  // first sample, end, left colour, right colour (0xBBGGRR)
+};
+
+// A free node and the nodes its curvature gradient reads: its neighbours
+// a, b and, where a neighbour is free, that neighbour's neighbours (-1 when
+// pinned), packed for one load.
+struct FreeNode {
+    int4 k_a_b_aa; // node, a, b, a's first neighbour
+    int4 ab_ba_bb; // a's second neighbour, b's neighbours, unused
+};
+
 struct StepArgs {
     const float2* x;     // positions read
     float2* y;           // positions written (Adam)
@@ -543,17 +566,22 @@ struct StepArgs {
     const float4* tgt;
     const int* flags;
     const int2* nbr;
+    const LiveSeg* live;
+    const float2* sxy;   // sample positions (source pixels), in segment order
+    const FreeNode* fnodes;
+    const RefineFrame* fr;
     float2* m;
     float2* v;
     double* energy;      // [3] when not NULL
-    int S, N, ow, scale;
-    float sig, inv_sig, cov_norm, curv_k, dev_k; // cov_norm = w_cov / (3 Ws Hs); curv_k = w_curv / F; dev_k = w_dev / F
+    float sigma;         // output pixels
+    float w_curv, w_dev, w_cov;
     float lr, bc1, bc2;  // Adam step and bias corrections 1 - beta^t
     int update;
 };
 
 constexpr float kBeta1 = 0.9f, kBeta2 = 0.999f, kEps = 1e-8f;
 constexpr float kInvSqrt2Pi = 0.3989422804014327f;
+constexpr int kSegLanes = 4; // lanes per segment in the coverage pass
 
 __device__ __forceinline__ float warp_sum(float v)
 {
@@ -562,51 +590,62 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-// One warp per segment: Chaikin ends from the nodes, every assigned sample's
-// soft colour, loss and d loss / d ends, reduced and pushed to the nodes.
+__device__ __forceinline__ float group_sum(float v, unsigned mask)
+{
+#pragma unroll
+    for (int o = kSegLanes / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    return v;
+}
+
+// Four lanes per live segment: Chaikin ends recomputed from the nodes, each
+// assigned sample's soft colour, loss and d loss / d ends, reduced in the
+// group and pushed to the segment's free nodes.
 __global__ void __launch_bounds__(256) k_rf_coverage(StepArgs a)
 {
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
+    const RefineFrame F = *a.fr;
+    const float inv_sig = (float)F.scale / a.sigma;
+    const float cov_norm = a.w_cov * F.inv_samples3;
+    const int lane = threadIdx.x & 31, gl = lane & (kSegLanes - 1);
+    const unsigned gmask = ((1u << kSegLanes) - 1u) << (lane & ~(kSegLanes - 1));
+    const int groups = (gridDim.x * blockDim.x) / kSegLanes;
     float eloss = 0.f;
-    for (int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < a.S; s += warps) {
-        const int4 sg = a.seg[s];
-        const int b0 = a.seg_off[s], b1 = a.seg_off[s + 1];
-        if (sg.w == SEG_NONE || b0 == b1) continue;
+    for (int l = (blockIdx.x * blockDim.x + threadIdx.x) / kSegLanes; l < F.L; l += groups) {
+        const LiveSeg ls = a.live[l];
+        const int4 sg = ls.nodes;
+        const int b0 = ls.range.x, b1 = ls.range.y;
         const int nodes[3] = {sg.x, sg.y, sg.z};
         float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (nodes[k] < 0) continue;
             const float2 p = a.x[nodes[k]];
-            const float wa = 0.25f * c_seg_wa[sg.w][k], wb = 0.25f * c_seg_wb[sg.w][k];
+            const float wa = 0.25f * seg_wa(sg.w, k), wb = 0.25f * seg_wb(sg.w, k);
             A.x += wa * p.x;
             A.y += wa * p.y;
             B.x += wb * p.x;
             B.y += wb * p.y;
         }
-        const uint2 c = a.col[s];
-        const float dl[3] = {(float)(int)(c.x & 0xFF) - (float)(int)(c.y & 0xFF),
-                             (float)(int)((c.x >> 8) & 0xFF) - (float)(int)((c.y >> 8) & 0xFF),
-                             (float)(int)((c.x >> 16) & 0xFF) - (float)(int)((c.y >> 16) & 0xFF)};
-        const float cr[3] = {(float)(c.y & 0xFF), (float)((c.y >> 8) & 0xFF), (float)((c.y >> 16) & 0xFF)};
+        const uint32_t cl = (uint32_t)ls.range.z, crr = (uint32_t)ls.range.w;
+        const float dl[3] = {(float)(int)(cl & 0xFF) - (float)(int)(crr & 0xFF),
+                             (float)(int)((cl >> 8) & 0xFF) - (float)(int)((crr >> 8) & 0xFF),
+                             (float)(int)((cl >> 16) & 0xFF) - (float)(int)((crr >> 16) & 0xFF)};
+        const float cr[3] = {(float)(crr & 0xFF), (float)((crr >> 8) & 0xFF), (float)((crr >> 16) & 0xFF)};
         const float ex = B.x - A.x, ey = B.y - A.y;
-        const float L2 = ex * ex + ey * ey, L = sqrtf(L2), invL = 1.f / L;
+        const float invL = rsqrtf(ex * ex + ey * ey);
         float gax = 0.f, gay = 0.f, gbx = 0.f, gby = 0.f;
-        for (int m = b0 + lane; m < b1; m += 32) {
-            const int xs = a.samp[m];
-            const float X = ((xs % a.ow) + 0.5f) / a.scale, Y = ((xs / a.ow) + 0.5f) / a.scale;
-            const float wx = X - A.x, wy = Y - A.y;
+        for (int m = b0 + gl; m < b1; m += kSegLanes) {
+            const float2 X = a.sxy[m];
+            const float wx = X.x - A.x, wy = X.y - A.y;
             const float d = (ex * wy - ey * wx) * invL;
-            const float z = d * a.inv_sig;
+            const float z = d * inv_sig;
             const float Phi = normcdff(z);
             const float4 t = a.tgt[m];
             const float r0 = (cr[0] + dl[0] * Phi - t.x) * (1.f / 255.f);
             const float r1 = (cr[1] + dl[1] * Phi - t.y) * (1.f / 255.f);
             const float r2 = (cr[2] + dl[2] * Phi - t.z) * (1.f / 255.f);
             eloss += r0 * r0 + r1 * r1 + r2 * r2;
-            const float phi = expf(-0.5f * z * z) * kInvSqrt2Pi * a.inv_sig;
-            const float dEdd = 2.f * a.cov_norm * (1.f / 255.f) * (r0 * dl[0] + r1 * dl[1] + r2 * dl[2]) * phi;
+            const float phi = expf(-0.5f * z * z) * kInvSqrt2Pi * inv_sig;
+            const float dEdd = 2.f * cov_norm * (1.f / 255.f) * (r0 * dl[0] + r1 * dl[1] + r2 * dl[2]) * phi;
             // d d / d e = (wy, -wx) / L - d e / L^2 ; d d / d w = (-ey, ex) / L
             const float dex = wy * invL - d * ex * invL * invL, dey = -wx * invL - d * ey * invL * invL;
             const float dwx = -ey * invL, dwy = ex * invL;
@@ -615,19 +654,20 @@ __global__ void __launch_bounds__(256) k_rf_coverage(StepArgs a)
             gax += dEdd * (-dex - dwx);
             gay += dEdd * (-dey - dwy);
         }
-        gax = warp_sum(gax);
-        gay = warp_sum(gay);
-        gbx = warp_sum(gbx);
-        gby = warp_sum(gby);
-        if (lane < 3 && nodes[lane] >= 0 && !(a.flags[nodes[lane]] & 1)) {
-            const float wa = 0.25f * c_seg_wa[sg.w][lane], wb = 0.25f * c_seg_wb[sg.w][lane];
-            atomicAdd(&a.gcov[nodes[lane]].x, wa * gax + wb * gbx);
-            atomicAdd(&a.gcov[nodes[lane]].y, wa * gay + wb * gby);
+        gax = group_sum(gax, gmask);
+        gay = group_sum(gay, gmask);
+        gbx = group_sum(gbx, gmask);
+        gby = group_sum(gby, gmask);
+        const int my = gl == 0 ? sg.x : (gl == 1 ? sg.y : (gl == 2 ? sg.z : -1));
+        if (my >= 0 && !(a.flags[my] & 1)) {
+            const float wa = 0.25f * seg_wa(sg.w, gl), wb = 0.25f * seg_wb(sg.w, gl);
+            atomicAdd(&a.gcov[my].x, wa * gax + wb * gbx);
+            atomicAdd(&a.gcov[my].y, wa * gay + wb * gby);
         }
     }
     if (a.energy) {
         eloss = warp_sum(eloss);
-        if (lane == 0 && eloss != 0.f) atomicAdd(&a.energy[2], (double)eloss * (double)a.cov_norm);
+        if (lane == 0 && eloss != 0.f) atomicAdd(&a.energy[2], (double)eloss * (double)cov_norm);
     }
 }
 
@@ -636,32 +676,32 @@ __global__ void __launch_bounds__(256) k_rf_coverage(StepArgs a)
 // gradient, then an Adam step (or the gradient written out).
 __global__ void __launch_bounds__(256) k_rf_nodes_step(StepArgs a)
 {
+    const RefineFrame F = *a.fr;
+    const float curv_k = a.w_curv / (float)max(F.F, 1), dev_k = a.w_dev / (float)max(F.F, 1);
     float ec = 0.f, ed = 0.f;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.N; k += gridDim.x * blockDim.x) {
-        if (a.flags[k] & 1) {
-            if (a.gout) a.gout[k] = make_float2(0.f, 0.f);
-            continue;
-        }
-        const float2 p = a.x[k];
-        const int2 nb = a.nbr[k];
-        const float2 pa = a.x[nb.x], pb = a.x[nb.y];
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F.F; f += gridDim.x * blockDim.x) {
+        const FreeNode fn = a.fnodes[f];
+        const int k = fn.k_a_b_aa.x;
+        const float2 p = a.x[k], pa = a.x[fn.k_a_b_aa.y], pb = a.x[fn.k_a_b_aa.z];
+        const int q_nb[4] = {fn.k_a_b_aa.w, fn.ab_ba_bb.x, fn.ab_ba_bb.y, fn.ab_ba_bb.z};
+        float2 qn[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) qn[t] = q_nb[t] >= 0 ? a.x[q_nb[t]] : make_float2(0.f, 0.f);
         const float tx = pa.x - 2.f * p.x + pb.x, ty = pa.y - 2.f * p.y + pb.y;
         float gx = -2.f * tx, gy = -2.f * ty;
-        const int q2[2] = {nb.x, nb.y};
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            const int q = q2[s];
-            if (a.flags[q] & 1) continue;
-            const int2 qn = a.nbr[q];
-            const float2 qa = a.x[qn.x], qq = a.x[q], qb = a.x[qn.y];
-            gx += qa.x - 2.f * qq.x + qb.x;
-            gy += qa.y - 2.f * qq.y + qb.y;
+        if (q_nb[0] >= 0) { // a is free: its second difference reads p
+            gx += qn[0].x - 2.f * pa.x + qn[1].x;
+            gy += qn[0].y - 2.f * pa.y + qn[1].y;
+        }
+        if (q_nb[2] >= 0) {
+            gx += qn[2].x - 2.f * pb.x + qn[3].x;
+            gy += qn[2].y - 2.f * pb.y + qn[3].y;
         }
         const float2 p0 = a.x0[k];
         const float dx = p.x - p0.x, dy = p.y - p0.y;
         const float2 gc = a.gcov[k];
-        gx = 0.25f * a.curv_k * gx + 2.f * a.dev_k * dx + gc.x;
-        gy = 0.25f * a.curv_k * gy + 2.f * a.dev_k * dy + gc.y;
+        gx = 0.25f * curv_k * gx + 2.f * dev_k * dx + gc.x;
+        gy = 0.25f * curv_k * gy + 2.f * dev_k * dy + gc.y;
         a.gcov[k] = make_float2(0.f, 0.f);
         if (a.energy) {
             ec += 0.125f * (tx * tx + ty * ty);
@@ -669,13 +709,13 @@ __global__ void __launch_bounds__(256) k_rf_nodes_step(StepArgs a)
         }
         if (a.gout) a.gout[k] = make_float2(gx, gy);
         if (a.update) {
-            float2 m = a.m[k], v = a.v[k];
+            float2 m = a.m[f], v = a.v[f];
             m.x = kBeta1 * m.x + (1.f - kBeta1) * gx;
             m.y = kBeta1 * m.y + (1.f - kBeta1) * gy;
             v.x = kBeta2 * v.x + (1.f - kBeta2) * gx * gx;
             v.y = kBeta2 * v.y + (1.f - kBeta2) * gy * gy;
-            a.m[k] = m;
-            a.v[k] = v;
+            a.m[f] = m;
+            a.v[f] = v;
             a.y[k] = make_float2(p.x - a.lr * (m.x / a.bc1) / (sqrtf(v.x / a.bc2) + kEps),
                                  p.y - a.lr * (m.y / a.bc1) / (sqrtf(v.y / a.bc2) + kEps));
         }
@@ -684,10 +724,50 @@ __global__ void __launch_bounds__(256) k_rf_nodes_step(StepArgs a)
         ec = warp_sum(ec);
         ed = warp_sum(ed);
         if ((threadIdx.x & 31) == 0) {
-            if (ec != 0.f) atomicAdd(&a.energy[0], (double)ec * (double)a.curv_k);
-            if (ed != 0.f) atomicAdd(&a.energy[1], (double)ed * (double)a.dev_k);
+            if (ec != 0.f) atomicAdd(&a.energy[0], (double)ec * (double)curv_k);
+            if (ed != 0.f) atomicAdd(&a.energy[1], (double)ed * (double)dev_k);
         }
     }
+}
+
+// live segments: a slot with a type and at least one sample
+__global__ void k_rf_live_flags(const int4* seg, const int* seg_off, int S, int* flag)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < S) flag[s] = seg[s].w != SEG_NONE && seg_off[s + 1] > seg_off[s];
+}
+
+__global__ void k_rf_live_scatter(const int* flag, const int* pos, int S, const int4* seg, const int* seg_off,
+                                  const uint2* col, LiveSeg* live)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < S && flag[s])
+        live[pos[s]] = LiveSeg{seg[s], make_int4(seg_off[s], seg_off[s + 1], (int)col[s].x, (int)col[s].y)};
+}
+
+__global__ void k_rf_sample_xy(const int* samp, int M, int ow, int scale, float2* sxy)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const int yo = samp[m] / ow, xo = samp[m] - yo * ow;
+    sxy[m] = make_float2(((float)xo + 0.5f) / (float)scale, ((float)yo + 0.5f) / (float)scale);
+}
+
+__global__ void k_rf_free_flags(const int* flags, int N, int* is_free)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < N) is_free[k] = !(flags[k] & 1);
+}
+
+__global__ void k_rf_free_nodes(const int* flags, const int2* nbr, const int* is_free, const int* pos, int N,
+                                FreeNode* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N || !is_free[k]) return;
+    const int2 nb = nbr[k];
+    const int2 na = (flags[nb.x] & 1) ? make_int2(-1, -1) : nbr[nb.x];
+    const int2 nbb = (flags[nb.y] & 1) ? make_int2(-1, -1) : nbr[nb.y];
+    out[pos[k]] = FreeNode{make_int4(k, nb.x, nb.y, na.x), make_int4(na.y, nbb.x, nbb.y, 0)};
 }
 
 template <typename T>
@@ -740,9 +820,22 @@ struct depix_refiner {
     DevBuf<int> bseg, seg_count, seg_off, cursor, samp;
     DevBuf<float4> tgt;
     DevBuf<double> energy;
+    DevBuf<LiveSeg> live;
+    DevBuf<int> live_flag, live_pos, free_flag, free_pos;
+    DevBuf<FreeNode> fnodes;
+    DevBuf<float2> sxy;
+    DevBuf<RefineFrame> frame;
+    int L = 0;
     int* h_scalars = nullptr; // pinned
     double* h_energy = nullptr;
+    RefineFrame* h_frame = nullptr;
     bool ready = false;
+    // the Adam loop as a graph, replayed while its parameters and buffers stay
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t loop = nullptr;
+    StepArgs loop_args{};
+    int loop_steps = -1;
+    int loop_cov_blocks = 0, loop_node_blocks = 0;
 };
 
 namespace {
@@ -801,18 +894,16 @@ StepArgs step_args(depix_refiner* r, const depix_refine_params* p)
     a.tgt = r->tgt.p;
     a.flags = r->node_flags.p;
     a.nbr = r->node_nbr.p;
+    a.live = r->live.p;
+    a.sxy = r->sxy.p;
+    a.fnodes = r->fnodes.p;
+    a.fr = r->frame.p;
     a.m = r->adam_m.p;
     a.v = r->adam_v.p;
-    a.S = r->S;
-    a.N = r->N;
-    a.ow = r->ow;
-    a.scale = r->scale;
-    a.sig = r->sigma / (float)r->scale;
-    a.inv_sig = 1.f / a.sig;
-    a.cov_norm = (float)((double)p->w_coverage / (3.0 * (double)r->ow * (double)r->oh));
-    const float F = (float)std::max(r->F, 1);
-    a.curv_k = p->w_curvature / F;
-    a.dev_k = p->w_deviation / F;
+    a.sigma = r->sigma;
+    a.w_curv = p->w_curvature;
+    a.w_dev = p->w_deviation;
+    a.w_cov = p->w_coverage;
     a.lr = p->lr;
     return a;
 }
@@ -836,8 +927,51 @@ depix_status check_sigma(const depix_refiner* r, const depix_refine_params* p)
     return DEPIX_OK;
 }
 
-int cov_blocks(const depix_refiner* r) { return std::max(1, std::min(r->sms * 8, blocks_for((long long)r->S * 32))); }
-int node_blocks(const depix_refiner* r) { return std::max(1, std::min(r->sms * 8, blocks_for(r->N))); }
+// grids: enough blocks for the frame rounded up to a power of two (the
+// kernels stride over the sizes they read on the device, so a captured loop
+// serves every frame whose rounded grids match), at most 8 blocks per SM
+int pow2_at_least(long long n)
+{
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+int cov_blocks(const depix_refiner* r)
+{
+    return std::min(r->sms * 8, pow2_at_least(((long long)r->L * kSegLanes + 255) / 256));
+}
+int node_blocks(const depix_refiner* r) { return std::min(r->sms * 8, pow2_at_least(((long long)r->F + 255) / 256)); }
+
+bool same_loop(const StepArgs& a, const StepArgs& b)
+{
+    return a.gcov == b.gcov && a.x0 == b.x0 && a.seg == b.seg && a.col == b.col && a.seg_off == b.seg_off &&
+           a.samp == b.samp && a.tgt == b.tgt && a.flags == b.flags && a.nbr == b.nbr && a.live == b.live && a.sxy == b.sxy && a.fnodes == b.fnodes &&
+           a.fr == b.fr && a.m == b.m && a.v == b.v && a.sigma == b.sigma && a.w_curv == b.w_curv &&
+           a.w_dev == b.w_dev && a.w_cov == b.w_cov && a.lr == b.lr;
+}
+
+// launches the Adam steps from pos_a (result in pos_a after an even number
+// of steps, pos_b after an odd one)
+cudaError_t launch_steps(depix_refiner* r, const StepArgs& base, int steps, cudaStream_t s)
+{
+    StepArgs a = base;
+    a.update = 1;
+    float2* x = r->pos_a.p;
+    float2* y = r->pos_b.p;
+    double b1 = 1.0, b2 = 1.0;
+    for (int t = 1; t <= steps; t++) {
+        b1 *= (double)kBeta1;
+        b2 *= (double)kBeta2;
+        a.x = x;
+        a.y = y;
+        a.bc1 = (float)(1.0 - b1);
+        a.bc2 = (float)(1.0 - b2);
+        k_rf_coverage<<<cov_blocks(r), 256, 0, s>>>(a);
+        k_rf_nodes_step<<<node_blocks(r), 256, 0, s>>>(a);
+        std::swap(x, y);
+    }
+    return cudaGetLastError();
+}
 
 // energy (and gradient when gout) at positions x, without an update
 depix_status eval(depix_refiner* r, const depix_refine_params* p, const float2* x, float2* gout, double out[4],
@@ -849,6 +983,7 @@ depix_status eval(depix_refiner* r, const depix_refine_params* p, const float2* 
     a.energy = r->energy.p;
     a.update = 0;
     RF_CK(cudaMemsetAsync(r->energy.p, 0, 3 * sizeof(double), s));
+    if (gout) RF_CK(cudaMemsetAsync(gout, 0, (size_t)r->N * sizeof(float2), s)); // pinned nodes stay zero
     k_rf_coverage<<<cov_blocks(r), 256, 0, s>>>(a);
     k_rf_nodes_step<<<node_blocks(r), 256, 0, s>>>(a);
     RF_CK(cudaGetLastError());
@@ -899,6 +1034,9 @@ depix_status depix_refiner_create(depix_refiner** out, size_t max_pixels)
     if (e == cudaSuccess) e = r->energy.reserve(3);
     if (e == cudaSuccess) e = cudaHostAlloc(&r->h_scalars, 8 * sizeof(int), cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaHostAlloc(&r->h_energy, 4 * sizeof(double), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&r->h_frame, sizeof(RefineFrame), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = r->frame.reserve(1);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGetLastError();
         depix_refiner_destroy(r);
@@ -922,6 +1060,11 @@ depix_status depix_refiner_destroy(depix_refiner* r)
     r->seg.release(); r->seg_col.release(); r->best.release(); r->bseg.release();
     r->seg_count.release(); r->seg_off.release(); r->cursor.release(); r->samp.release(); r->tgt.release();
     r->energy.release();
+    r->live.release(); r->live_flag.release(); r->live_pos.release(); r->frame.release();
+    r->free_flag.release(); r->free_pos.release(); r->fnodes.release(); r->sxy.release();
+    if (r->loop) cudaGraphExecDestroy(r->loop);
+    if (r->capture_stream) cudaStreamDestroy(r->capture_stream);
+    cudaFreeHost(r->h_frame);
     cudaFreeHost(r->h_scalars);
     cudaFreeHost(r->h_energy);
     delete r;
@@ -1020,9 +1163,18 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     k_rf_sort_samples<<<blocks_for(S), 256, 0, s>>>(r->seg_off.p, S, r->samp.p);
     k_rf_targets<<<blocks_for(M), 256, 0, s>>>(G, p->scale, (double)rp->sigma / p->scale, r->samp.p, M, r->tgt.p);
     RF_CK(cudaGetLastError());
-    // free nodes
-    RF_CK(cudaMemsetAsync(r->scalars.p + 3, 0, sizeof(int), s));
-    k_rf_count_free<<<blocks_for(N), 256, 0, s>>>(r->node_flags.p, N, r->scalars.p + 3);
+    RF_CK(r->sxy.reserve(M));
+    k_rf_sample_xy<<<blocks_for(M), 256, 0, s>>>(r->samp.p, M, ow, p->scale, r->sxy.p);
+    // free nodes and their curvature stencils
+    RF_CK(r->free_flag.reserve(N));
+    RF_CK(r->free_pos.reserve(N));
+    RF_CK(r->fnodes.reserve(N));
+    k_rf_free_flags<<<blocks_for(N), 256, 0, s>>>(r->node_flags.p, N, r->free_flag.p);
+    RF_CK(cudaGetLastError());
+    RF_CK(exclusive_scan(r->free_flag.p, r->free_pos.p, N, r->tile_sums.p, r->scalars.p + 3, s));
+    k_rf_free_nodes<<<blocks_for(N), 256, 0, s>>>(r->node_flags.p, r->node_nbr.p, r->free_flag.p, r->free_pos.p, N,
+                                                  r->fnodes.p);
+    RF_CK(cudaGetLastError());
     RF_CK(cudaMemsetAsync(r->gcov.p, 0, (size_t)std::max(N, 1) * sizeof(float2), s));
     int F = 0;
     DEPIX_TRY_RF(read_total(r, 3, &F, s));
@@ -1037,6 +1189,22 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     r->S = S;
     r->M = M;
     r->sigma = rp->sigma;
+    // live segments
+    RF_CK(r->live_flag.reserve(S));
+    RF_CK(r->live_pos.reserve(S));
+    RF_CK(r->live.reserve(S));
+    k_rf_live_flags<<<blocks_for(S), 256, 0, s>>>(r->seg.p, r->seg_off.p, S, r->live_flag.p);
+    RF_CK(cudaGetLastError());
+    RF_CK(exclusive_scan(r->live_flag.p, r->live_pos.p, S, r->tile_sums.p, r->scalars.p + 4, s));
+    k_rf_live_scatter<<<blocks_for(S), 256, 0, s>>>(r->live_flag.p, r->live_pos.p, S, r->seg.p, r->seg_off.p,
+                                                    r->seg_col.p, r->live.p);
+    RF_CK(cudaGetLastError());
+    int L = 0;
+    DEPIX_TRY_RF(read_total(r, 4, &L, s));
+    r->L = L;
+    *r->h_frame = RefineFrame{N, L, ow, oh, p->scale, F, (float)(1.0 / (3.0 * (double)ow * (double)oh))};
+    RF_CK(cudaMemcpyAsync(r->frame.p, r->h_frame, sizeof(RefineFrame), cudaMemcpyHostToDevice, s));
+    RF_CK(cudaStreamSynchronize(s));
     r->ready = true;
     return DEPIX_OK;
 }
@@ -1135,22 +1303,38 @@ depix_status depix_refine_run(depix_refiner* r, const depix_refine_params* p, fl
     RF_CK(cudaMemsetAsync(r->adam_m.p, 0, bytes, s));
     RF_CK(cudaMemsetAsync(r->adam_v.p, 0, bytes, s));
     if (before) DEPIX_TRY_RF(eval(r, p, x, nullptr, before, s));
-    StepArgs a = step_args(r, p);
-    a.update = 1;
-    const int cb = cov_blocks(r), nb = node_blocks(r);
-    double b1 = 1.0, b2 = 1.0;
-    for (int t = 1; t <= p->steps; t++) {
-        b1 *= (double)kBeta1;
-        b2 *= (double)kBeta2;
-        a.x = x;
-        a.y = y;
-        a.bc1 = (float)(1.0 - b1);
-        a.bc2 = (float)(1.0 - b2);
-        k_rf_coverage<<<cb, 256, 0, s>>>(a);
-        k_rf_nodes_step<<<nb, 256, 0, s>>>(a);
-        std::swap(x, y);
+    const StepArgs a = step_args(r, p);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RF_CK(cudaStreamIsCapturing(s, &cs));
+    if (p->steps > 0 && cs == cudaStreamCaptureStatusNone) {
+        if (!r->loop || r->loop_steps != p->steps || !same_loop(a, r->loop_args) ||
+            r->loop_args.x != r->pos_a.p || r->loop_args.y != r->pos_b.p || r->loop_cov_blocks != cov_blocks(r) ||
+            r->loop_node_blocks != node_blocks(r)) {
+            if (r->loop) cudaGraphExecDestroy(r->loop);
+            r->loop = nullptr;
+            RF_CK(cudaStreamBeginCapture(r->capture_stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = launch_steps(r, a, p->steps, r->capture_stream);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(r->capture_stream, &g);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&r->loop, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                r->loop = nullptr;
+                return rf_fail(e, "refine loop capture");
+            }
+            r->loop_args = a;
+            r->loop_args.x = r->pos_a.p;
+            r->loop_args.y = r->pos_b.p;
+            r->loop_steps = p->steps;
+            r->loop_cov_blocks = cov_blocks(r);
+            r->loop_node_blocks = node_blocks(r);
+        }
+        RF_CK(cudaGraphLaunch(r->loop, s));
+    } else {
+        RF_CK(launch_steps(r, a, p->steps, s));
     }
-    RF_CK(cudaGetLastError());
+    if (p->steps & 1) x = y;
     if (after) DEPIX_TRY_RF(eval(r, p, x, nullptr, after, s));
     if (d_pos) RF_CK(cudaMemcpyAsync(d_pos, x, bytes, cudaMemcpyDeviceToDevice, s));
     return DEPIX_OK;

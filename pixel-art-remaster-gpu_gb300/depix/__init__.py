@@ -304,13 +304,14 @@ class Refiner:
                                               stream_ptr(stream)), "depix_refine_energy_grad")
         return tuple(e)
 
-    def run(self, rp, pos=None, stream=None):
-        """Adam; returns (energy before, energy after) as 4-tuples."""
+    def run(self, rp, pos=None, stream=None, energies=True):
+        """Adam; returns (energy before, energy after) as 4-tuples, or None
+        without the (synchronising) energy evaluations."""
         b = (ctypes.c_double * 4)()
         a = (ctypes.c_double * 4)()
-        _check(lib().depix_refine_run(self.handle, ctypes.byref(rp), ptr(pos), b, a, stream_ptr(stream)),
-               "depix_refine_run")
-        return tuple(b), tuple(a)
+        _check(lib().depix_refine_run(self.handle, ctypes.byref(rp), ptr(pos), b if energies else None,
+                                      a if energies else None, stream_ptr(stream)), "depix_refine_run")
+        return (tuple(b), tuple(a)) if energies else None
 
 
 def launch_kernel_compat(pos, col, img_host, w, h, ws, edge_count_host, graph_host, subdivide, p=None):
