@@ -69,6 +69,7 @@ struct Geo {
     int w, h;
     int gw, gh;         // vertex grid: (4w + 3) x (4h + 3), origin at quarter (-1, -1)
     const uint64_t* lut;
+    const uint32_t* box; // per-pattern hull boxes (k_rf_boxes)
     uint32_t thr;
 };
 
@@ -114,19 +115,29 @@ __device__ __forceinline__ uint32_t cell_word(const Geo& G, int i, int j)
     return word_of_bgr(load_bgr(G.img, G.ws, G.layout, i, j));
 }
 
-// Walks the split edges of cell idx. For each: owner direction of the twin
-// (-1: none) and the twin cell. fn(ux, uy, vx, vy, owner, B).
+// Walks the split edges of cell idx; for each, the twin's owner: the first
+// 8-neighbour (in bit order) with a hull edge that holds the reversed split
+// edge. A neighbour is only searched when its hull's bounding box (the
+// per-pattern box table) holds the split edge. fn(ux, uy, vx, vy, owner, B).
 template <typename Fn>
 __device__ void walk_split_edges(const Geo& G, const uint32_t* vgrid, int idx, Fn fn)
 {
     const int i = idx % G.w, j = idx / G.w;
     const uint64_t e = cell_hull(G, idx);
     const int k = (int)(e & 0xF);
-    uint64_t nh[8];
+    int npat[8];
+    uint32_t nbox[8]; // x0, x1, y0, y1 in global quarter units, 8 bits each after a +8 bias
 #pragma unroll
     for (int d = 0; d < 8; d++) {
         const int ni = i + dir_di(d), nj = j + dir_dj(d);
-        nh[d] = (ni >= 0 && ni < G.w && nj >= 0 && nj < G.h) ? cell_hull(G, nj * G.w + ni) : 0ull;
+        npat[d] = -1;
+        nbox[d] = 0;
+        if (ni >= 0 && ni < G.w && nj >= 0 && nj < G.h) {
+            const int nidx = nj * G.w + ni;
+            const int n = G.w * G.h;
+            npat[d] = cell_pattern(G.g[nidx], nidx > 0 ? G.g[nidx - 1] : 0u, nidx + 1 < n ? G.g[nidx + 1] : 0u);
+            nbox[d] = __ldg(&G.box[npat[d]]);
+        }
     }
     for (int t = 0; t < k; t++) {
         const int t1 = t + 1 == k ? 0 : t + 1;
@@ -138,10 +149,19 @@ __device__ void walk_split_edges(const Geo& G, const uint32_t* vgrid, int idx, F
             const int cx = ax + st * sx, cy = ay + st * sy;
             if (st < gcd && !(vgrid[vindex(G, cx, cy)] & kVUsed)) continue;
             int owner = -1;
+            // the split edge relative to the cell's own quarter origin
+            const int lx0 = min(px, cx) - 4 * i, lx1 = max(px, cx) - 4 * i;
+            const int ly0 = min(py, cy) - 4 * j, ly1 = max(py, cy) - 4 * j;
             for (int d = 0; d < 8 && owner < 0; d++) {
-                const uint64_t ne = nh[d];
-                const int nk = (int)(ne & 0xF);
+                if (npat[d] < 0) continue;
+                const uint32_t bb = nbox[d];
+                const int ox = 4 * dir_di(d), oy = 4 * dir_dj(d);
+                if (lx0 < (int)(bb & 0xFF) - 8 + ox || lx1 > (int)((bb >> 8) & 0xFF) - 8 + ox ||
+                    ly0 < (int)((bb >> 16) & 0xFF) - 8 + oy || ly1 > (int)(bb >> 24) - 8 + oy)
+                    continue;
                 const int ni = i + dir_di(d), nj = j + dir_dj(d);
+                const uint64_t ne = __ldg(&G.lut[npat[d]]);
+                const int nk = (int)(ne & 0xF);
                 for (int s = 0; s < nk; s++) {
                     const int s1 = s + 1 == nk ? 0 : s + 1;
                     if (reversed_on(qvx(ne, s, ni), qvy(ne, s, nj), qvx(ne, s1, ni), qvy(ne, s1, nj), px, py, cx, cy)) {
@@ -156,6 +176,25 @@ __device__ void walk_split_edges(const Geo& G, const uint32_t* vgrid, int idx, F
             py = cy;
         }
     }
+}
+
+// per pattern: the hull's bounding box in local quarter units, each bound + 8
+__global__ void k_rf_boxes(const uint64_t* lut, uint32_t* box)
+{
+    const int pat = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pat >= 4096) return;
+    const uint64_t e = lut[pat];
+    const int k = (int)(e & 0xF);
+    int x0 = 99, x1 = -99, y0 = 99, y1 = -99;
+    for (int t = 0; t < k; t++) {
+        const int x = qvx(e, t, 0), y = qvy(e, t, 0);
+        x0 = min(x0, x);
+        x1 = max(x1, x);
+        y0 = min(y0, y);
+        y1 = max(y1, y);
+    }
+    box[pat] = k ? (uint32_t)(x0 + 8) | (uint32_t)(x1 + 8) << 8 | (uint32_t)(y0 + 8) << 16 | (uint32_t)(y1 + 8) << 24
+                 : 0xFFu; // empty: x0 beyond every edge
 }
 
 __global__ void k_rf_mark_vertices(Geo G, uint32_t* vgrid)
@@ -329,14 +368,24 @@ __device__ __forceinline__ void seg_ends(const int4 sg, const int2* q, int scale
     by *= m;
 }
 
+// squared distance, or -1 beyond the band (decided in integers first, so the
+// rounded division only runs for samples inside it)
 __device__ __forceinline__ double seg_dist2(long long ax, long long ay, long long bx, long long by, long long X,
                                             long long Y)
 {
+    const long long band2 = (long long)kBand * kBand;
     const long long ex = bx - ax, ey = by - ay, wx = X - ax, wy = Y - ay;
     const long long L = ex * ex + ey * ey, dot = ex * wx + ey * wy;
-    if (dot <= 0) return (double)(wx * wx + wy * wy);
-    if (dot >= L) return (double)((X - bx) * (X - bx) + (Y - by) * (Y - by));
+    if (dot <= 0) {
+        const long long d = wx * wx + wy * wy;
+        return d <= band2 ? (double)d : -1.0;
+    }
+    if (dot >= L) {
+        const long long d = (X - bx) * (X - bx) + (Y - by) * (Y - by);
+        return d <= band2 ? (double)d : -1.0;
+    }
     const long long cr = ex * wy - ey * wx;
+    if (cr * cr > band2 * L) return -1.0;
     return __ddiv_rn((double)(cr * cr), (double)L);
 }
 
@@ -356,7 +405,7 @@ __device__ void seg_samples(const int4 sg, const int2* q, int scale, int ow, int
     for (long long yo = y0; yo <= y1; yo++)
         for (long long xo = x0; xo <= x1; xo++) {
             const double d2 = seg_dist2(ax, ay, bx, by, 16 * (2 * xo + 1), 16 * (2 * yo + 1));
-            if (d2 <= (double)(kBand * kBand)) fn((int)(yo * ow + xo), d2);
+            if (d2 >= 0.0) fn((int)(yo * ow + xo), d2);
         }
 }
 
@@ -416,30 +465,40 @@ __global__ void k_rf_sort_samples(const int* seg_off, int S, int* samp)
 }
 
 // the nearest-neighbour target under the coverage Gaussian, per sample
-__global__ void k_rf_targets(Geo G, int scale, double sig, const int* samp, int M, float4* tgt)
+// (separable: three column and three row weights)
+__global__ void k_rf_targets(Geo G, int scale, float sig, const int* samp, int M, float4* tgt)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     const int ow = G.w * scale;
-    const int xo = samp[m] % ow, yo = samp[m] / ow;
-    const double x = (xo + 0.5) / scale, y = (yo + 0.5) / scale;
+    const int yo = samp[m] / ow, xo = samp[m] - yo * ow;
+    const float x = ((float)xo + 0.5f) / (float)scale, y = ((float)yo + 0.5f) / (float)scale;
     const int ix = xo / scale, iy = yo / scale;
-    double r = 0, g = 0, b = 0;
-    for (int dj = -1; dj <= 1; dj++) {
-        const int jj = iy + dj;
+    const float inv = 1.f / sig;
+    float cx[3], cy[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int ii = ix + d - 1, jj = iy + d - 1;
+        cx[d] = (ii >= 0 && ii < G.w) ? normcdff((x - (float)ii) * inv) - normcdff((x - (float)ii - 1.f) * inv) : 0.f;
+        cy[d] = (jj >= 0 && jj < G.h) ? normcdff((y - (float)jj) * inv) - normcdff((y - (float)jj - 1.f) * inv) : 0.f;
+    }
+    float r = 0.f, g = 0.f, b = 0.f;
+#pragma unroll
+    for (int dj = 0; dj < 3; dj++) {
+        const int jj = iy + dj - 1;
         if (jj < 0 || jj >= G.h) continue;
-        const double cy = normcdf((y - jj) / sig) - normcdf((y - jj - 1) / sig);
-        for (int di = -1; di <= 1; di++) {
-            const int ii = ix + di;
+#pragma unroll
+        for (int di = 0; di < 3; di++) {
+            const int ii = ix + di - 1;
             if (ii < 0 || ii >= G.w) continue;
-            const double cx = normcdf((x - ii) / sig) - normcdf((x - ii - 1) / sig);
+            const float wgt = cx[di] * cy[dj];
             const uint32_t c = cell_rgb(G, jj * G.w + ii);
-            r += cx * cy * (double)(c & 0xFF);
-            g += cx * cy * (double)((c >> 8) & 0xFF);
-            b += cx * cy * (double)((c >> 16) & 0xFF);
+            r += wgt * (float)(c & 0xFF);
+            g += wgt * (float)((c >> 8) & 0xFF);
+            b += wgt * (float)((c >> 16) & 0xFF);
         }
     }
-    tgt[m] = make_float4((float)r, (float)g, (float)b, 0.f);
+    tgt[m] = make_float4(r, g, b, 0.f);
 }
 
 // ---------------------------------------------------------------- scans
@@ -808,6 +867,7 @@ struct depix_refiner {
     int E = 0, N = 0, F = 0, S = 0, M = 0;
     float sigma = 0.5f; // coverage sigma of the targets (output pixels)
     DevBuf<uint32_t> vgrid;
+    DevBuf<uint32_t> box;
     DevBuf<int> cell_count, cell_off, is_node, nid, tile_sums, scalars;
     DevBuf<int2> nb_v, nb_e;
     DevBuf<int4> edges;
@@ -1030,6 +1090,12 @@ depix_status depix_refiner_create(depix_refiner** out, size_t max_pixels)
     cudaError_t e = cudaGetDevice(&r->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, r->device);
     if (e == cudaSuccess) e = hull_table_address(&r->lut);
+    if (e == cudaSuccess) e = r->box.reserve(4096);
+    if (e == cudaSuccess) {
+        k_rf_boxes<<<16, 256>>>(r->lut, r->box.p);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     if (e == cudaSuccess) e = r->scalars.reserve(8);
     if (e == cudaSuccess) e = r->energy.reserve(3);
     if (e == cudaSuccess) e = cudaHostAlloc(&r->h_scalars, 8 * sizeof(int), cudaHostAllocDefault);
@@ -1051,6 +1117,7 @@ depix_status depix_refiner_destroy(depix_refiner* r)
 {
     if (!r) return DEPIX_OK;
     r->vgrid.release();
+    r->box.release();
     r->cell_count.release(); r->cell_off.release(); r->is_node.release(); r->nid.release();
     r->tile_sums.release(); r->scalars.release();
     r->nb_v.release(); r->nb_e.release(); r->edges.release();
@@ -1095,7 +1162,8 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     cudaStream_t s = reinterpret_cast<cudaStream_t>(s_);
     r->ready = false;
     const int n = w * h, gw = 4 * w + 3, gh = 4 * h + 3, nv = gw * gh;
-    Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, pack_thresholds(p->tr_y, p->tr_u, p->tr_v)};
+    Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, r->box.p,
+          pack_thresholds(p->tr_y, p->tr_u, p->tr_v)};
     RF_CK(r->vgrid.reserve(nv));
     RF_CK(r->cell_count.reserve(n));
     RF_CK(r->cell_off.reserve(n));
@@ -1161,7 +1229,7 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     RF_CK(cudaMemsetAsync(r->cursor.p, 0, ((size_t)S + 1) * sizeof(int), s));
     k_rf_scatter_samples<<<blocks_for(no_px), 256, 0, s>>>(r->bseg.p, no_px, r->seg_off.p, r->cursor.p, r->samp.p);
     k_rf_sort_samples<<<blocks_for(S), 256, 0, s>>>(r->seg_off.p, S, r->samp.p);
-    k_rf_targets<<<blocks_for(M), 256, 0, s>>>(G, p->scale, (double)rp->sigma / p->scale, r->samp.p, M, r->tgt.p);
+    k_rf_targets<<<blocks_for(M), 256, 0, s>>>(G, p->scale, rp->sigma / (float)p->scale, r->samp.p, M, r->tgt.p);
     RF_CK(cudaGetLastError());
     RF_CK(r->sxy.reserve(M));
     k_rf_sample_xy<<<blocks_for(M), 256, 0, s>>>(r->samp.p, M, ow, p->scale, r->sxy.p);
