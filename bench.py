@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--sprites", type=int, default=4096, help="sprites in the uneven-batch leg")
     ap.add_argument("--no-sprites", action="store_true")
     ap.add_argument("--no-refine", action="store_true")
+    ap.add_argument("--no-stream", action="store_true")
+    ap.add_argument("--stream-frames", type=int, default=512)
     return ap.parse_args()
 
 
@@ -293,6 +295,7 @@ def run_ours(args, rank, world, local_rank):
 
     sprites = None if args.no_sprites else run_sprites(args, dev, stream)
     refine = None if args.no_refine else run_refine(args, dev, stream, cpu=(rank == 0 and world == 1 and not args.no_cpu))
+    stream_leg = None if args.no_stream else run_stream(args, dev, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -310,7 +313,7 @@ def run_ours(args, rank, world, local_rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
-                "refine": refine}
+                "refine": refine, "stream": stream_leg}
         print(json.dumps(line))
 
 
@@ -464,6 +467,128 @@ def run_refine(args, dev, stream, cpu):
                                "sample": f"{k} Adam steps of the float64 numpy specification "
                                          f"(oracle/refine_oracle.py) on the same frame and topology"}
     return out
+
+
+def run_stream(args, dev, stream):
+    """A stream of 256x224 frames (background + 24 moving sprites), x4: the
+    plain path (one depix_frame call per frame) against batches of 8 through
+    depix_batch followed, per frame, by topology setup, a warm start from the
+    previous frame's refined nodes (tiles with unchanged signatures) and 20
+    Adam steps. Frame latency: from the batch's (or frame's) upload to its
+    last kernel; uploads from pinned host memory are inside the timed region."""
+    import numpy as np
+    import torch
+    import depix
+    from depix import synth
+
+    n = args.stream_frames
+    B = 8
+    frames = synth.stream(n, seed=0)
+    h_frames = torch.from_numpy(frames.reshape(n, -1)).pin_memory()
+    fb = W * H * 4
+    out_px = W * H * SCALE * SCALE
+    p = depix.params(48, 7, 6, True, SCALE)
+    rp = depix.refine_params(steps=20)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    # plain: one frame at a time
+    ctx1 = depix.Context(W * H, 1)
+    d_in1 = torch.empty(fb, dtype=torch.uint8, device=dev)
+    d_out1 = torch.empty(out_px * 4, dtype=torch.uint8, device=dev)
+    for f in range(3):
+        d_in1.copy_(h_frames[f], non_blocking=True)
+        ctx1.frame(d_in1, W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out1, None, None, stream=stream)
+    torch.cuda.synchronize()
+    marks = [(ev(), ev()) for _ in range(n)]
+    t0 = time.perf_counter()
+    for f in range(n):
+        a, b = marks[f]
+        a.record(stream)
+        d_in1.copy_(h_frames[f], non_blocking=True)
+        ctx1.frame(d_in1, W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out1, None, None, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_lat = sorted(a.elapsed_time(b) for a, b in marks)
+    ctx1.close()
+
+    # batched + refined with warm start
+    ctx = depix.Context(W * H, B)
+    d_in = torch.empty(B * fb, dtype=torch.uint8, device=dev)
+    d_out = torch.empty(B * out_px * 4, dtype=torch.uint8, device=dev)
+    rfs = [depix.Refiner(W * H), depix.Refiner(W * H)]
+    cap = 4 * W * H  # nodes never exceed a few per pixel
+    pos = [torch.empty(2 * cap, dtype=torch.float32, device=dev) for _ in range(2)]
+    in_off = [k * fb for k in range(B)]
+    out_off = [k * out_px * 4 for k in range(B)]
+
+    def run_all(count_reuse):
+        reused, tiles = 0, 0
+        prev = None
+        for b0 in range(0, n, B):
+            start = ev()
+            start.record(stream)
+            d_in.copy_(h_frames[b0:b0 + B].reshape(-1), non_blocking=True)
+            ctx.batch([W] * B, [H] * B, in_off, out_off, d_in, p, d_out, None, stream=stream)
+            for k in range(B):
+                f = b0 + k
+                rf, ps = rfs[f % 2], pos[f % 2]
+                rf.setup(d_in[k * fb:], W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp, stream=stream)
+                assert rf.counts()["nodes"] <= cap
+                if prev is None:
+                    rf.initial(ps, stream=stream)
+                else:
+                    r = rf.warm_start(rfs[prev % 2], pos[prev % 2], ps, stream=stream, count=count_reuse)
+                    if count_reuse:
+                        reused += r
+                        tiles += ((W + 15) // 16) * ((H + 15) // 16)
+                rf.run(rp, ps, stream=stream, energies=False)
+                done = ev()
+                done.record(stream)
+                lat_marks.append((start, done))
+                prev = f
+        return reused, tiles
+
+    lat_marks = []
+    run_all(False)  # warm-up pass
+    torch.cuda.synchronize()
+    lat_marks = []
+    t0 = time.perf_counter()
+    run_all(False)
+    torch.cuda.synchronize()
+    batched_s = time.perf_counter() - t0
+    lat = sorted(a.elapsed_time(b) for a, b in lat_marks)
+    lat_marks = []
+    reused, tiles = run_all(True)
+    torch.cuda.synchronize()
+
+    # warm against cold start: energy after 20 steps on a few frames
+    warm_e, cold_e = [], []
+    for f in range(1, 17):
+        rf, ps = rfs[f % 2], pos[f % 2]
+        prv = rfs[(f - 1) % 2]
+        prv.setup(torch.from_numpy(frames[f - 1].reshape(-1)).to(dev), W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp,
+                  stream=stream)
+        pp = pos[(f - 1) % 2]
+        prv.initial(pp, stream=stream)
+        prv.run(depix.refine_params(steps=200), pp, stream=stream, energies=False)
+        rf.setup(torch.from_numpy(frames[f].reshape(-1)).to(dev), W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp,
+                 stream=stream)
+        rf.warm_start(prv, pp, ps, stream=stream, count=False)
+        warm_e.append(rf.run(rp, ps, stream=stream)[1][3])
+        cold_e.append(rf.run(rp, None, stream=stream)[1][3])
+    for r in rfs:
+        r.close()
+    ctx.close()
+    pct = lambda v, q: round(v[min(len(v) - 1, int(q * len(v)))], 4)
+    return {"workload": f"{n} frames 256x224 (background + 24 sprites at 0-3 px/frame, wrap-around), x4; "
+                        f"refinement: 20 Adam steps per frame, warm start by 16x16 tile signature",
+            "plain": {"frames_per_s": round(n / plain_s, 1), "p50_ms": pct(plain_lat, 0.5),
+                      "p99_ms": pct(plain_lat, 0.99)},
+            "batched_refined": {"frames_per_s": round(n / batched_s, 1), "p50_ms": pct(lat, 0.5),
+                                "p99_ms": pct(lat, 0.99), "batch": B, "reused_tile_frac": round(reused / max(tiles, 1), 4)},
+            "energy_after_20_steps": {"warm_start": round(float(np.mean(warm_e)), 6),
+                                      "cold_start": round(float(np.mean(cold_e)), 6), "frames": len(warm_e)}}
 
 
 # ---------------------------------------------------------- reference arm

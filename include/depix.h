@@ -251,9 +251,11 @@ void depix_refine_default_params(depix_refine_params* p);
 depix_status depix_refiner_create(depix_refiner** r, size_t max_pixels);
 depix_status depix_refiner_destroy(depix_refiner* r);
 /* Extracts and freezes one frame's topology from its image and resolved
- * graph (p: thresholds of the curve test, output scale 1..12): nodes, curve
- * edges, Chaikin segments, the output samples near each segment and their
- * targets. Synchronises the stream (reads counts back). */
+ * graph (p: thresholds of the curve test, output scale 1..12; d_graph NULL:
+ * the refiner resolves the graph itself): nodes, curve edges, Chaikin
+ * segments, the output samples near each segment and their targets, and a
+ * signature per 16x16-pixel tile (graph bytes and colours of the tile and its
+ * one-pixel ring). Synchronises the stream (reads counts back). */
 depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, int h, int widthstep,
                                 depix_layout layout, const uint8_t* d_graph, const depix_params* p,
                                 const depix_refine_params* rp, depix_stream s);
@@ -268,6 +270,13 @@ depix_status depix_refine_export(depix_refiner* r, int32_t* node_q, int32_t* nod
                                  int32_t* edges, int32_t* segs, uint32_t* seg_colors, int32_t* samples);
 /* Start positions (float x, y per node, source pixels) to d_pos. */
 depix_status depix_refine_initial(depix_refiner* r, float* d_pos, depix_stream s);
+/* Warm start from the previous frame of a stream (same size): nodes in tiles
+ * whose signature is unchanged take prev's position (d_prev_pos, prev's node
+ * order) of the node at the same quarter-pixel coordinates; every other node
+ * its start position. Writes r's start positions to d_pos; reused_tiles (may
+ * be NULL; reading it synchronises) gets the number of unchanged tiles. */
+depix_status depix_refine_warm_start(depix_refiner* r, const depix_refiner* prev, const float* d_prev_pos,
+                                     float* d_pos, int* reused_tiles, depix_stream s);
 /* Energy terms (curvature, deviation, coverage, total) at d_pos and, when
  * d_grad is set, dE/d position per node (zero at pinned nodes): the adjoint.
  * Synchronous. */

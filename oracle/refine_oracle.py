@@ -280,6 +280,46 @@ def seg_dist2(ax, ay, bx, by, X, Y):
     return np.where(dot <= 0, d_a, np.where(dot >= L, d_b, mid))
 
 
+# -------------------------------------------------------------- warm start
+
+WARM_TILE = 16
+
+
+def tile_signatures(img, graph):
+    """FNV-1a (64-bit) per 16x16 tile over the resolved graph byte and the
+    RGB of each pixel of the tile and its one-pixel ring, row-major, pixels
+    outside the frame skipped."""
+    h, w = img.shape[:2]
+    tx, ty = -(-w // WARM_TILE), -(-h // WARM_TILE)
+    g = graph.reshape(h, w)
+    out = []
+    for t in range(tx * ty):
+        x0, y0 = (t % tx) * WARM_TILE - 1, (t // tx) * WARM_TILE - 1
+        hsh = 0xCBF29CE484222325
+        for y in range(max(y0, 0), min(y0 + WARM_TILE + 2, h)):
+            for x in range(max(x0, 0), min(x0 + WARM_TILE + 2, w)):
+                for byte in (int(g[y, x]), int(img[y, x, 0]), int(img[y, x, 1]), int(img[y, x, 2])):
+                    hsh = ((hsh ^ byte) * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+        out.append(hsh)
+    return out, tx
+
+
+def warm_positions(top, sig, prev_top, prev_sig, prev_pos, tiles_x):
+    """Start positions of `top` warm-started from the previous frame: a node
+    in a tile whose signature is unchanged takes the previous position of the
+    node at the same quarter coordinates, if there is one."""
+    prev = {(int(x), int(y)): k for k, (x, y) in enumerate(zip(prev_top.qx, prev_top.qy))}
+    P = initial_positions(top)
+    for k, (x, y) in enumerate(zip(top.qx, top.qy)):
+        px = min(max(int(x) >> 2, 0), top.w - 1)
+        py = min(max(int(y) >> 2, 0), top.h - 1)
+        t = (py // WARM_TILE) * tiles_x + px // WARM_TILE
+        j = prev.get((int(x), int(y)))
+        if sig[t] == prev_sig[t] and j is not None:
+            P[k] = prev_pos[j]
+    return P
+
+
 # ------------------------------------------------------------------ energy
 
 

@@ -501,6 +501,66 @@ __global__ void k_rf_targets(Geo G, int scale, float sig, const int* samp, int M
     tgt[m] = make_float4(r, g, b, 0.f);
 }
 
+// ------------------------------------------------------------ warm start
+
+constexpr int kWarmTile = 16; // source pixels per tile side
+
+// Tile signature: FNV-1a (64-bit) over the resolved graph byte and the RGB of
+// every pixel of the tile and its one-pixel ring (row-major, pixels outside
+// the frame skipped): everything the tile's cells, curve edges and targets
+// depend on.
+__global__ void k_rf_tile_hash(Geo G, int tiles_x, int tiles, uint64_t* hash)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tiles) return;
+    const int x0 = (t % tiles_x) * kWarmTile - 1, y0 = (t / tiles_x) * kWarmTile - 1;
+    uint64_t hsh = 0xcbf29ce484222325ull;
+    auto mix = [&](uint32_t byte) {
+        hsh ^= byte;
+        hsh *= 0x100000001b3ull;
+    };
+    for (int y = max(y0, 0); y < min(y0 + kWarmTile + 2, G.h); y++)
+        for (int x = max(x0, 0); x < min(x0 + kWarmTile + 2, G.w); x++) {
+            const int idx = y * G.w + x;
+            const uint32_t c = cell_rgb(G, idx);
+            mix(G.g[idx]);
+            mix(c & 0xFF);
+            mix((c >> 8) & 0xFF);
+            mix((c >> 16) & 0xFF);
+        }
+    hash[t] = hsh;
+}
+
+__global__ void k_rf_warm_scatter(const int2* q, const float2* pos, int N, int gw, float2* grid, int* stamp, int epoch)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int v = (q[k].y + 1) * gw + (q[k].x + 1);
+    grid[v] = pos[k];
+    stamp[v] = epoch;
+}
+
+__global__ void k_rf_warm_gather(const int2* q, const float2* pos0, int N, int w, int h, int gw, int tiles_x,
+                                 const uint64_t* hash, const uint64_t* prev_hash, const float2* grid,
+                                 const int* stamp, int epoch, float2* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const int2 c = q[k];
+    const int px = min(max(c.x >> 2, 0), w - 1), py = min(max(c.y >> 2, 0), h - 1);
+    const int t = (py / kWarmTile) * tiles_x + px / kWarmTile;
+    const int v = (c.y + 1) * gw + (c.x + 1);
+    out[k] = (hash[t] == prev_hash[t] && stamp[v] == epoch) ? grid[v] : pos0[k];
+}
+
+__global__ void k_rf_same_tiles(const uint64_t* a, const uint64_t* b, int tiles, int* count)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool same = t < tiles && a[t] == b[t];
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, same);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, __popc(m));
+}
+
 // ---------------------------------------------------------------- scans
 
 constexpr int kScanBlock = 1024, kScanItems = 4, kScanTile = kScanBlock * kScanItems;
@@ -868,6 +928,11 @@ struct depix_refiner {
     float sigma = 0.5f; // coverage sigma of the targets (output pixels)
     DevBuf<uint32_t> vgrid;
     DevBuf<uint32_t> box;
+    DevBuf<uint8_t> own_graph, own_snap; // resolved graph when the caller gives none
+    DevBuf<uint64_t> tile_hash;
+    DevBuf<float2> warm_grid;
+    DevBuf<int> warm_stamp;
+    int tiles_x = 0, tiles = 0, warm_epoch = 0;
     DevBuf<int> cell_count, cell_off, is_node, nid, tile_sums, scalars;
     DevBuf<int2> nb_v, nb_e;
     DevBuf<int4> edges;
@@ -1118,6 +1183,8 @@ depix_status depix_refiner_destroy(depix_refiner* r)
     if (!r) return DEPIX_OK;
     r->vgrid.release();
     r->box.release();
+    r->own_graph.release(); r->own_snap.release(); r->tile_hash.release(); r->warm_grid.release();
+    r->warm_stamp.release();
     r->cell_count.release(); r->cell_off.release(); r->is_node.release(); r->nid.release();
     r->tile_sums.release(); r->scalars.release();
     r->nb_v.release(); r->nb_e.release(); r->edges.release();
@@ -1143,7 +1210,7 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
                                 const depix_refine_params* rp, depix_stream s_)
 {
     DEPIX_TRY_RF(check_rparams(rp));
-    if (!r || !d_img || !d_graph || !p || w < 1 || h < 1) {
+    if (!r || !d_img || !p || w < 1 || h < 1) {
         set_last_error("refine setup: NULL argument or size below 1");
         return DEPIX_ERR_INVALID_ARG;
     }
@@ -1162,6 +1229,15 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     cudaStream_t s = reinterpret_cast<cudaStream_t>(s_);
     r->ready = false;
     const int n = w * h, gw = 4 * w + 3, gh = 4 * h + 3, nv = gw * gh;
+    if (!d_graph) {
+        // the frame's resolved graph: similarity + trivial, then heuristics
+        RF_CK(r->own_graph.reserve(n));
+        RF_CK(r->own_snap.reserve(n));
+        const FrameBatch fb{d_img, 0, r->own_snap.p, 0, w, h, widthstep, (int)layout};
+        RF_CK(launch_graph(fb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+        RF_CK(launch_heuristics(GraphBatch{r->own_snap.p, r->own_graph.p, 0, w, h}, 1, s));
+        d_graph = r->own_graph.p;
+    }
     Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, r->box.p,
           pack_thresholds(p->tr_y, p->tr_u, p->tr_v)};
     RF_CK(r->vgrid.reserve(nv));
@@ -1267,6 +1343,11 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     k_rf_live_scatter<<<blocks_for(S), 256, 0, s>>>(r->live_flag.p, r->live_pos.p, S, r->seg.p, r->seg_off.p,
                                                     r->seg_col.p, r->live.p);
     RF_CK(cudaGetLastError());
+    r->tiles_x = (w + kWarmTile - 1) / kWarmTile;
+    r->tiles = r->tiles_x * ((h + kWarmTile - 1) / kWarmTile);
+    RF_CK(r->tile_hash.reserve(r->tiles));
+    k_rf_tile_hash<<<blocks_for(r->tiles, 64), 64, 0, s>>>(G, r->tiles_x, r->tiles, r->tile_hash.p);
+    RF_CK(cudaGetLastError());
     int L = 0;
     DEPIX_TRY_RF(read_total(r, 4, &L, s));
     r->L = L;
@@ -1337,6 +1418,43 @@ depix_status depix_refine_initial(depix_refiner* r, float* d_pos, depix_stream s
     }
     RF_CK(cudaMemcpyAsync(d_pos, r->pos0.p, (size_t)r->N * sizeof(float2), cudaMemcpyDeviceToDevice,
                           reinterpret_cast<cudaStream_t>(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_refine_warm_start(depix_refiner* r, const depix_refiner* prev, const float* d_prev_pos,
+                                     float* d_pos, int* reused_tiles, depix_stream s_)
+{
+    DEPIX_TRY_RF(check_refiner(r));
+    if (!prev || !prev->ready || !d_prev_pos || !d_pos) {
+        set_last_error("warm start: previous refiner without a frame, or NULL positions");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    if (prev->w != r->w || prev->h != r->h) {
+        set_last_error("warm start: the previous frame has another size");
+        return DEPIX_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(s_);
+    const int gw = 4 * r->w + 3, nv = gw * (4 * r->h + 3);
+    if (r->warm_grid.cap < (size_t)nv || !r->warm_grid.p) {
+        RF_CK(r->warm_grid.reserve(nv));
+        RF_CK(r->warm_stamp.reserve(nv));
+        RF_CK(cudaMemsetAsync(r->warm_stamp.p, 0, (size_t)nv * sizeof(int), s));
+        r->warm_epoch = 0;
+    }
+    const int epoch = ++r->warm_epoch;
+    k_rf_warm_scatter<<<blocks_for(prev->N), 256, 0, s>>>(prev->node_q.p, reinterpret_cast<const float2*>(d_prev_pos),
+                                                          prev->N, gw, r->warm_grid.p, r->warm_stamp.p, epoch);
+    k_rf_warm_gather<<<blocks_for(r->N), 256, 0, s>>>(r->node_q.p, r->pos0.p, r->N, r->w, r->h, gw, r->tiles_x,
+                                                      r->tile_hash.p, prev->tile_hash.p, r->warm_grid.p,
+                                                      r->warm_stamp.p, epoch, reinterpret_cast<float2*>(d_pos));
+    RF_CK(cudaGetLastError());
+    if (reused_tiles) {
+        RF_CK(cudaMemsetAsync(r->scalars.p + 5, 0, sizeof(int), s));
+        k_rf_same_tiles<<<blocks_for(r->tiles), 256, 0, s>>>(r->tile_hash.p, prev->tile_hash.p, r->tiles,
+                                                             r->scalars.p + 5);
+        RF_CK(cudaGetLastError());
+        DEPIX_TRY_RF(read_total(r, 5, reused_tiles, s));
+    }
     return DEPIX_OK;
 }
 

@@ -95,6 +95,7 @@ def lib():
         _sig(L, "depix_refine_export", [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp])
         _sig(L, "depix_refine_initial", [_vp, _vp, _vp])
         _sig(L, "depix_refine_energy_grad", [_vp, RP, _vp, _vp, _vp, _vp])
+        _sig(L, "depix_refine_warm_start", [_vp, _vp, _vp, _vp, _vp, _vp])
         _sig(L, "depix_refine_run", [_vp, RP, _vp, _vp, _vp, _vp])
         _sig(L, "depix_yuv_words", [_vp, ctypes.c_size_t, _vp, _vp])
         _sig(L, "depix_pattern_tables", [_vp, _vp])
@@ -297,6 +298,15 @@ class Refiner:
 
     def initial(self, pos, stream=None):
         _check(lib().depix_refine_initial(self.handle, ptr(pos), stream_ptr(stream)), "depix_refine_initial")
+
+    def warm_start(self, prev, prev_pos, pos, stream=None, count=True):
+        """Start positions from the previous frame's refiner; returns the
+        number of unchanged tiles (None with count=False)."""
+        n = ctypes.c_int(0)
+        _check(lib().depix_refine_warm_start(self.handle, prev.handle, ptr(prev_pos), ptr(pos),
+                                             ctypes.byref(n) if count else None, stream_ptr(stream)),
+               "depix_refine_warm_start")
+        return n.value if count else None
 
     def energy_grad(self, rp, pos, grad=None, stream=None):
         e = (ctypes.c_double * 4)()

@@ -13,12 +13,14 @@ image loader flips rows, Image.cpp:21-38).
 * ``sprites`` -- a list of sprites with sides drawn from U[8, 64], 4-16
                  colours, 1-8 shapes; 30 % have a fully transparent background
                  and outlined shapes.
+* ``stream``  -- frames of a 256x224 background (``frame``) with 24 sprites
+                 moving at integer velocities of 0-3 px/frame, wrapping around.
 """
 from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["frame", "frame_large", "sprites", "draw_scene", "rgba_to_bgr"]
+__all__ = ["frame", "frame_large", "sprites", "stream", "draw_scene", "rgba_to_bgr"]
 
 
 def _outline(img, mask, color):
@@ -112,6 +114,31 @@ def sprites(count: int = 4096, seed: int = 0, lo: int = 8, hi: int = 64):
         transparent = bool(rng.random() < 0.3)
         out.append(draw_scene(rng, w, h, n_colors, n_rect, n_shapes - n_rect, size_lo=4,
                               size_hi=min(48, max(w, h)), dither_frac=0.05, transparent_bg=transparent))
+    return out
+
+
+def stream(n_frames: int, seed: int = 0, n_sprites: int = 24, w: int = 256, h: int = 224):
+    """``n_frames`` frames: the background ``frame(seed)`` with ``n_sprites``
+    sprites of the ``sprites`` generator on top, each moving by an integer
+    velocity (vx, vy in 0..3 px/frame) and wrapping around the frame edges.
+    Sprite pixels with alpha 0 show the background. Returns (n, h, w, 4)."""
+    rng = np.random.default_rng([0xDE91, 3, seed])
+    bg = frame(seed, w=w, h=h)
+    sp = sprites(n_sprites, seed=seed + 1000)
+    pos = [(int(rng.integers(0, w)), int(rng.integers(0, h))) for _ in sp]
+    vel = [(int(rng.integers(0, 4)), int(rng.integers(0, 4))) for _ in sp]
+    out = np.empty((n_frames, h, w, 4), np.uint8)
+    for f in range(n_frames):
+        img = bg.copy()
+        for s_img, (x0, y0), (vx, vy) in zip(sp, pos, vel):
+            sh, sw = s_img.shape[:2]
+            ys = (y0 + vy * f + np.arange(sh)) % h
+            xs = (x0 + vx * f + np.arange(sw)) % w
+            opaque = s_img[..., 3] > 0
+            region = img[np.ix_(ys, xs)]
+            region[opaque] = s_img[opaque]
+            img[np.ix_(ys, xs)] = region
+        out[f] = img
     return out
 
 

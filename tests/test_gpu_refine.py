@@ -227,3 +227,52 @@ def test_setup_rejects_bad_arguments(cuda):
     with pytest.raises(depix.DepixError):
         rf.energy_grad(depix.refine_params(sigma=1.0), pos)
     rf.close()
+
+
+def test_warm_start_from_the_previous_frame(cuda):
+    """Two frames of a stream: the second warm-starts from the first's
+    refined nodes in tiles whose signature is unchanged (checked against the
+    float64 specification's rule and its own tile signatures)."""
+    import depix
+    torch = cuda
+    frames = synth.stream(3, seed=2, n_sprites=2, w=128, h=96)  # 19 of 48 tiles unchanged
+    a, b = frames[0], frames[2]
+    rfa, rp, raw_a, res_a = _setup(torch, a)
+    rfb, _, raw_b, res_b = _setup(torch, b)
+    top_a = R.topology(a, res_a, raw_a, 4)
+    top_b = R.topology(b, res_b, raw_b, 4)
+    pos_a = torch.empty(2 * len(top_a.qx), dtype=torch.float32, device="cuda")
+    rfa.initial(pos_a)
+    rfa.run(depix.refine_params(steps=50), pos_a)
+    pos_b = torch.empty(2 * len(top_b.qx), dtype=torch.float32, device="cuda")
+    reused = rfb.warm_start(rfa, pos_a, pos_b)
+    sig_a, tx = R.tile_signatures(a, res_a)
+    sig_b, _ = R.tile_signatures(b, res_b)
+    same = sum(x == y for x, y in zip(sig_a, sig_b))
+    assert reused == same and 0 < same < len(sig_a)
+    want = R.warm_positions(top_b, sig_b, top_a, sig_a, pos_a.cpu().numpy().reshape(-1, 2).astype(np.float64), tx)
+    got = pos_b.cpu().numpy().reshape(-1, 2).astype(np.float64)
+    assert np.array_equal(got, want)
+    moved = np.any(want != R.initial_positions(top_b), axis=1)
+    assert moved.sum() > 10  # some nodes really carried over
+    # refinement from the warm start
+    before, after = rfb.run(depix.refine_params(steps=20), pos_b)
+    assert after[3] < before[3]
+    rfa.close()
+    rfb.close()
+
+
+def test_setup_resolves_the_graph_itself(cuda):
+    import depix
+    torch = cuda
+    img = synth.frame(3, w=64, h=40)
+    rf, rp, raw, res = _setup(torch, img)
+    g1 = rf.export()
+    d_img = torch.from_numpy(np.ascontiguousarray(img).reshape(-1).copy()).cuda()
+    rf2 = depix.Refiner(64 * 40)
+    rf2.setup(d_img, 64, 40, 256, depix.LAYOUT_RGBA, None, depix.params(), rp)
+    g2 = rf2.export()
+    for k in g1:
+        assert np.array_equal(g1[k], g2[k]), k
+    rf.close()
+    rf2.close()
