@@ -180,6 +180,7 @@ def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
     import depix
+    from depix import replicas
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -226,12 +227,9 @@ def run_ours(args, rank, world, local_rank):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     stages = ctx.stage_times()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    frames_total = B * args.steps * world
-    value = frames_total / (ms / 1e3)
+    # replicas: every rank ran its own B frames per step; the job's time is the slowest rank's
+    ms = replicas.max_over_ranks(ms, dev)
+    value = replicas.job_throughput(B * args.steps, ms / 1e3, dev)
 
     # roofline of the kernel that writes the output (the raster stage: one
     # kernel per call); algorithmic bytes: image and graph in, raster out
@@ -261,11 +259,8 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(e2e_steps):
         ctx.batch_host(ws, hs, in_off, out_off, h_in, h_in.numel(), p, h_out, h_out.numel(), h_lab, stream=stream)
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": round(B * e2e_steps * world / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": B * in_bytes,
+    e2e_v = replicas.job_throughput(B * e2e_steps, e2e_s, dev)
+    e2e = {"value": round(e2e_v, 1), "unit": UNIT, "h2d_bytes_per_step": B * in_bytes,
            "d2h_bytes_per_step": B * (out_px * 4 + W * H * 4), "steps": e2e_steps}
     # spot check of the e2e output against the device path
     assert torch.equal(h_out[: out_px * 4], d_out[: out_px * 4].cpu()), "e2e output differs from device path"
