@@ -596,6 +596,26 @@ __device__ __forceinline__ int floor_div(int a, int b) // b > 0
     return (a % b != 0 && a < 0) ? q - 1 : q;
 }
 
+// floor(a / b) and a - b * floor(a / b) for b > 0, |a| < 2^30, |a / b| < 2^20:
+// a float estimate (off by less than one: a loses at most 2^6 in the
+// conversion, b >= 256 in every use, relative error 2^-23) corrected once in
+// each direction with exact integer arithmetic.
+__device__ __forceinline__ int floor_div_fast(int a, int b, int& rem)
+{
+    int q = __float2int_rd(__fdividef((float)a, (float)b));
+    int r = a - q * b;
+    if (r < 0) {
+        q--;
+        r += b;
+    }
+    if (r >= b) {
+        q++;
+        r -= b;
+    }
+    rem = r;
+    return q;
+}
+
 // True when every edge turns strictly counter-clockwise around the cell
 // centre (32, 32) and the polygon winds around it exactly once: the vertices
 // are then in increasing angle around the centre, so the polygon is
@@ -648,8 +668,9 @@ __device__ __forceinline__ void crossing_mask(const Packed& P, int u, int mlo, i
         // samples left of the crossing: 256 m + 128 < x_cross  <=>  m < num / den
         int num = lx * D + (256 * r0 + 128 - ly) * (hxx - lx) - 128 * D;
         const int step = 256 * (hxx - lx);
-        int q = floor_div(num, den), r = num - q * den;
-        const int sq = floor_div(step, den), sr = step - sq * den;
+        int r, sr;
+        int q = floor_div_fast(num, den, r);
+        const int sq = floor_div_fast(step, den, sr);
         for (int row = r0; row <= r1; row++) {
             const int k = q + (r > 0 ? 1 : 0) - mlo; // ceil(num / den) - mlo
             rows[(row - mlo) * rstride] ^= k <= 0 ? 0u : (k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u));
