@@ -194,9 +194,9 @@ def run_ours(args, rank, world, local_rank):
     d_lab = torch.empty(B * W * H, dtype=torch.int32, device=dev)
     ctx = depix.Context(W * H, B)
     p = depix.params(48, 7, 6, True, SCALE)
-    ws, hs = [W] * B, [H] * B
-    in_off = [k * in_bytes for k in range(B)]
-    out_off = [k * out_px * 4 for k in range(B)]
+    ws, hs = np.full(B, W, np.int32), np.full(B, H, np.int32)
+    in_off = np.arange(B, dtype=np.uint64) * np.uint64(in_bytes)
+    out_off = np.arange(B, dtype=np.uint64) * np.uint64(out_px * 4)
     stream = torch.cuda.current_stream(dev)
 
     def step():
@@ -330,6 +330,9 @@ def run_sprites(args, dev, stream):
         out_off.append(oo)
         oi += (w * h * 4 + 15) // 16 * 16
         oo += (w * h * 64 + 15) // 16 * 16
+    # per-frame arrays as numpy: the binding passes them by pointer
+    ws_a, hs_a = np.array(ws, np.int32), np.array(hs, np.int32)
+    in_a, out_a = np.array(in_off, np.uint64), np.array(out_off, np.uint64)
     buf = np.zeros(oi, np.uint8)
     for k, img in enumerate(imgs):
         buf[in_off[k]:in_off[k] + img.size] = img.reshape(-1)
@@ -341,7 +344,7 @@ def run_sprites(args, dev, stream):
     ctx = depix.Context(64 * 64, len(imgs))
 
     def step():
-        ctx.batch(ws, hs, in_off, out_off, d_in, p, d_out, d_lab, stream=stream)
+        ctx.batch(ws_a, hs_a, in_a, out_a, d_in, p, d_out, d_lab, stream=stream)
 
     t0 = time.perf_counter()
     step()  # tunes the launch shape for this size bucket

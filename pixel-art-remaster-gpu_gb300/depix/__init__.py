@@ -211,9 +211,18 @@ class Context:
 
     @staticmethod
     def _arrays(ws, hs, in_off, out_off):
+        """ctypes views of the per-frame arrays: numpy int32 / uint64 arrays
+        pass by pointer (no per-call conversion), other sequences are copied."""
+        import numpy as np
         n = len(ws)
-        return (n, (ctypes.c_int * n)(*ws), (ctypes.c_int * n)(*hs), (ctypes.c_uint64 * n)(*in_off),
-                (ctypes.c_uint64 * n)(*out_off))
+
+        def view(a, dtype, ctype):
+            if isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.c_contiguous:
+                return a.ctypes.data_as(ctypes.POINTER(ctype))
+            return (ctype * n)(*a)
+
+        return (n, view(ws, np.int32, ctypes.c_int), view(hs, np.int32, ctypes.c_int),
+                view(in_off, np.uint64, ctypes.c_uint64), view(out_off, np.uint64, ctypes.c_uint64))
 
     def batch(self, ws, hs, in_off, out_off, img, p, out, labels=None, stream=None):
         """ws/hs/in_off/out_off: host int sequences (frame sizes, byte offsets)."""
