@@ -1,5 +1,6 @@
 // depix_api.cu -- host side of the C ABI: argument checks, per-device
 // set-up, the frame/batch drivers and the drop-in launch_kernel.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -342,6 +343,9 @@ struct depix_context {
     double ms[DEPIX_STAGE_COUNT] = {};
     long long launches[DEPIX_STAGE_COUNT] = {};
     long long calls[DEPIX_STAGE_COUNT] = {};
+    // host-buffer batches: copy-back stream and per-chunk events
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> chunk_done;
     // uneven batches (created on the first one)
     QueueRunner* queue = nullptr;
     bool shape_forced = false;
@@ -545,6 +549,75 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
     return DEPIX_OK;
 }
 
+// ---- host-buffer batches in chunks: the copy back of one chunk overlaps the
+// upload and the kernels of the next (the device-to-host link, not the
+// kernels, bounds a host-buffer batch of x4 rasters)
+
+constexpr int kMinChunkFrames = 16, kMaxChunks = 8;
+
+// frames in order, each input and output range after the previous one's
+bool frames_in_order(int n, const int* w, const int* h, const uint64_t* in_offset, const uint64_t* out_offset,
+                     int scale)
+{
+    for (int k = 1; k < n; k++) {
+        const uint64_t ib = (uint64_t)w[k - 1] * h[k - 1] * 4, ob = ib * (uint64_t)scale * scale;
+        if (in_offset[k] < in_offset[k - 1] + ib || out_offset[k] < out_offset[k - 1] + ob) return false;
+    }
+    return true;
+}
+
+BatchShape chunk_shape(int n, const int* w, const int* h, const uint64_t* in_offset, const uint64_t* out_offset)
+{
+    BatchShape sh;
+    for (int k = 0; k < n; k++) {
+        if (w[k] != w[0] || h[k] != h[0]) sh.uniform = false;
+        sh.total_pixels += (size_t)w[k] * h[k];
+    }
+    for (int k = 2; k < n; k++)
+        if (in_offset[k] - in_offset[k - 1] != in_offset[1] - in_offset[0] ||
+            out_offset[k] - out_offset[k - 1] != out_offset[1] - out_offset[0])
+            sh.strided = false;
+    return sh;
+}
+
+depix_status batch_host_pipelined(depix_context* ctx, int n, const int* w, const int* h, const uint64_t* in_offset,
+                                  const uint64_t* out_offset, const uint8_t* h_img, const depix_params* p,
+                                  uint8_t* h_out, int32_t* h_labels, cudaStream_t s)
+{
+    if (!ctx->copy_stream) DEPIX_CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while ((int)ctx->chunk_done.size() < kMaxChunks + 1) {
+        cudaEvent_t e = nullptr;
+        DEPIX_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->chunk_done.push_back(e);
+    }
+    const int chunks = std::min(kMaxChunks, n / kMinChunkFrames);
+    const size_t s2 = (size_t)p->scale * p->scale;
+    size_t lab = 0;
+    for (int c = 0; c < chunks; c++) {
+        const int a = (int)((long long)n * c / chunks), b = (int)((long long)n * (c + 1) / chunks);
+        const size_t ib_last = (size_t)w[b - 1] * h[b - 1] * 4;
+        const size_t in0 = in_offset[a], in1 = in_offset[b - 1] + ib_last;
+        const size_t out0 = out_offset[a], out1 = out_offset[b - 1] + ib_last * s2;
+        DEPIX_CK(cudaMemcpyAsync(ctx->stage_in + in0, h_img + in0, in1 - in0, cudaMemcpyHostToDevice, s));
+        const BatchShape sh = chunk_shape(b - a, w + a, h + a, in_offset + a, out_offset + a);
+        DEPIX_TRY(run_batch(ctx, b - a, w + a, h + a, in_offset + a, out_offset + a, ctx->stage_in, p,
+                            ctx->stage_out, h_labels ? ctx->stage_labels + lab : nullptr, sh, s));
+        DEPIX_CK(cudaEventRecord(ctx->chunk_done[c], s));
+        DEPIX_CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[c], 0));
+        DEPIX_CK(cudaMemcpyAsync(h_out + out0, ctx->stage_out + out0, out1 - out0, cudaMemcpyDeviceToHost,
+                                 ctx->copy_stream));
+        if (h_labels)
+            DEPIX_CK(cudaMemcpyAsync(h_labels + lab, ctx->stage_labels + lab, sh.total_pixels * sizeof(int32_t),
+                                     cudaMemcpyDeviceToHost, ctx->copy_stream));
+        lab += sh.total_pixels;
+    }
+    // the caller's stream resumes after the last copy
+    DEPIX_CK(cudaEventRecord(ctx->chunk_done[kMaxChunks], ctx->copy_stream));
+    DEPIX_CK(cudaStreamWaitEvent(s, ctx->chunk_done[kMaxChunks], 0));
+    DEPIX_CK(cudaStreamSynchronize(s));
+    return DEPIX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -581,6 +654,11 @@ depix_status depix_context_destroy(depix_context* c)
     cudaFree(c->stage_out);
     cudaFree(c->stage_labels);
     if (c->queue) queue_runner_destroy(c->queue);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    for (auto e : c->chunk_done) cudaEventDestroy(e);
     for (auto& m : c->marks) {
         cudaEventDestroy(m.a);
         cudaEventDestroy(m.b);
@@ -718,6 +796,12 @@ depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int
     }
     DEPIX_TRY(ensure_staging(ctx, in_bytes, out_bytes, h_labels ? shape.total_pixels : 0));
     cudaStream_t s = S(s_);
+    if (n >= 2 * kMinChunkFrames && frames_in_order(n, w, h, in_offset, out_offset, p->scale)) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        DEPIX_CK(cudaStreamIsCapturing(s, &cs));
+        if (cs == cudaStreamCaptureStatusNone)
+            return batch_host_pipelined(ctx, n, w, h, in_offset, out_offset, h_img, p, h_out, h_labels, s);
+    }
     DEPIX_CK(cudaMemcpyAsync(ctx->stage_in, h_img, in_bytes, cudaMemcpyHostToDevice, s));
     DEPIX_TRY(run_batch(ctx, n, w, h, in_offset, out_offset, ctx->stage_in, p, ctx->stage_out,
                         h_labels ? ctx->stage_labels : nullptr, shape, s));

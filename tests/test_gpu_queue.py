@@ -228,3 +228,31 @@ def test_scale_beyond_the_mask_raster_uses_per_frame_launches(cuda):
     rasters, labs = _run(torch, ctx, imgs, 13)
     _check(imgs, 13, rasters, labs)
     ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["uniform", "uneven"])
+def test_host_batch_in_chunks_equals_the_device_batch(cuda, kind):
+    """Batches of 32 or more frames in order go through depix_batch_host in
+    chunks whose copy-back overlaps the next chunk's kernels: same bytes as
+    the device-buffer call, labels included."""
+    import depix
+    torch = cuda
+    if kind == "uniform":
+        imgs = [synth.frame(90 + k, w=40, h=24) for k in range(48)]
+    else:
+        imgs = synth.sprites(40, seed=77)
+    buf, in_off, out_off, out_bytes = _pack(imgs, 4)
+    ws, hs = [i.shape[1] for i in imgs], [i.shape[0] for i in imgs]
+    npx = sum(w * h for w, h in zip(ws, hs))
+    ctx = depix.Context(max(w * h for w, h in zip(ws, hs)), len(imgs))
+    d_out = torch.zeros(out_bytes, dtype=torch.uint8, device="cuda")
+    d_lab = torch.zeros(npx, dtype=torch.int32, device="cuda")
+    ctx.batch(ws, hs, in_off, out_off, torch.from_numpy(buf).cuda(), depix.params(), d_out, d_lab)
+    h_out = torch.zeros(out_bytes, dtype=torch.uint8).pin_memory()
+    h_lab = torch.zeros(npx, dtype=torch.int32).pin_memory()
+    h_in = torch.from_numpy(buf).pin_memory()
+    ctx.batch_host(ws, hs, in_off, out_off, h_in, buf.size, depix.params(), h_out, out_bytes, h_lab)
+    torch.cuda.synchronize()
+    assert torch.equal(h_out, d_out.cpu())
+    assert torch.equal(h_lab, d_lab.cpu())
+    ctx.close()
