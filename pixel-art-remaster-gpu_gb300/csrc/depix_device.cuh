@@ -686,6 +686,62 @@ __device__ __forceinline__ void crossing_mask(const Packed& P, int u, int mlo, i
     for (int row = 0; row < F; row++) rows[row * rstride] &= fmask;
 }
 
+// star_simple, the polygon's bounding box and crossing_mask in one pass over
+// the vertices. Returns star_simple's answer; the rows are only meaningful
+// when it is true (the caller clears them and ear-clips otherwise).
+__device__ __forceinline__ bool star_crossing_mask(const Packed& P, int u, int mlo, int F, uint32_t* rows, int rstride,
+                                                   int& mnx, int& mny, int& mxx, int& mxy)
+{
+    const int n = P.n;
+    int px = pk_get(P.x0, P.x1, n - 1), py = pk_get(P.y0, P.y1, n - 1);
+    mnx = mxx = px;
+    mny = mxy = py;
+    bool ok = n >= 3;
+    int wraps = 0;
+    for (int i = 0; i < n; i++) {
+        const int x = pk_get(P.x0, P.x1, i), y = pk_get(P.y0, P.y1, i);
+        mnx = min(mnx, x);
+        mxx = max(mxx, x);
+        mny = min(mny, y);
+        mxy = max(mxy, y);
+        // star test about the cell centre
+        const int cx0 = px - kUnit / 2, cy0 = py - kUnit / 2, cx1 = x - kUnit / 2, cy1 = y - kUnit / 2;
+        ok &= cx0 * cy1 - cy0 * cx1 > 0;
+        const bool up_prev = cy0 > 0 || (cy0 == 0 && cx0 > 0), up = cy1 > 0 || (cy1 == 0 && cx1 > 0);
+        wraps += (!up_prev && up) ? 1 : 0;
+        // crossings of the edge prev -> this vertex
+        const int ax = px * u, ay = py * u, bx = x * u, by = y * u;
+        px = x;
+        py = y;
+        if (ay == by) continue;
+        int lx = ax, ly = ay, hxx = bx, hyy = by;
+        if (ly > hyy) {
+            lx = bx; ly = by; hxx = ax; hyy = ay;
+        }
+        const int r0 = max(((ly - 128) >> 8) + 1, mlo), r1 = min((hyy - 128) >> 8, mlo + F - 1);
+        if (r0 > r1) continue;
+        const int D = hyy - ly, den = 256 * D;
+        int num = lx * D + (256 * r0 + 128 - ly) * (hxx - lx) - 128 * D;
+        const int step = 256 * (hxx - lx);
+        int r, sr;
+        int q = floor_div_fast(num, den, r);
+        const int sq = floor_div_fast(step, den, sr);
+        for (int row = r0; row <= r1; row++) {
+            const int k = q + (r > 0 ? 1 : 0) - mlo;
+            rows[(row - mlo) * rstride] ^= k <= 0 ? 0u : (k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u));
+            q += sq;
+            r += sr;
+            if (r >= den) {
+                r -= den;
+                q++;
+            }
+        }
+    }
+    const uint32_t fmask = F >= 32 ? 0xFFFFFFFFu : ((1u << F) - 1u);
+    for (int row = 0; row < F; row++) rows[row * rstride] &= fmask;
+    return ok && wraps == 1;
+}
+
 }  // namespace depix
 
 namespace depix {

@@ -748,17 +748,12 @@ __device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const Ma
     subdivide_tables(pat, e, nb_pattern, tj, sp);
     for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
     const int u = 4 * Gm.s;
-    if (star_simple(sp)) {
-        // the reference's ear clip would tile the polygon exactly
-        crossing_mask(sp, u, Gm.mlo, Gm.F, rows, rstride);
-    } else if (ear_clip_mask(sp, u, Gm.mlo, Gm.F, rows, rstride) == 0) {
-        return 0;
-    }
-    int mnx = 1 << 20, mny = 1 << 20, mxx = -(1 << 20), mxy = -(1 << 20);
-    for (int t = 0; t < sp.n; t++) {
-        const int x = pk_get(sp.x0, sp.x1, t), y = pk_get(sp.y0, sp.y1, t);
-        mnx = min(mnx, x); mxx = max(mxx, x);
-        mny = min(mny, y); mxy = max(mxy, y);
+    int mnx, mny, mxx, mxy;
+    // a star-shaped polygon is simple: the reference's ear clip would tile it
+    // exactly, so its crossing-number mask is the coverage
+    if (!star_crossing_mask(sp, u, Gm.mlo, Gm.F, rows, rstride, mnx, mny, mxx, mxy)) {
+        for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
+        if (ear_clip_mask(sp, u, Gm.mlo, Gm.F, rows, rstride) == 0) return 0;
     }
     return spill_bits(mnx, mny, mxx, mxy);
 }
