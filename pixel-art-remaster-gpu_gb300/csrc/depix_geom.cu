@@ -628,8 +628,9 @@ struct MaskTile {
     uint32_t pix[CH][CW];
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
     uint8_t live[GN];  // the cell exists (inside the image)
-    uint16_t list[GN]; // subdivided cells of the tile
+    uint16_t list[GN]; // subdivided cells of the tile, then the blocks that need owner resolution
     int count;
+    int slow;          // blocks in list for the owner-resolution pass
 };
 
 __device__ __forceinline__ uint32_t rgba_of(uint32_t p)
@@ -768,7 +769,10 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
     const MaskGeom G = mask_geom(s);
     const int F = G.F;
     // ---- phase A
-    if (threadIdx.x == 0) M.count = 0;
+    if (threadIdx.x == 0) {
+        M.count = 0;
+        M.slow = 0;
+    }
     for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
         int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
         unsigned v = 0;
@@ -856,20 +860,32 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         const uint32_t* own = masks + (size_t)k0 * F;
         bool full = true;
         for (int r = 0; r < s; r++) full &= ((own[r - G.mlo] >> (-G.mlo)) & blockbits) == blockbits;
-        const uint32_t own_col = rgba_of(M.pix[ty + 2][tx + 2]);
-        uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
-        if (full && !intr) {
-            for (int r = 0; r < s; r++) {
-                uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
-                if (vec) {
-                    for (int c4 = 0; c4 < s; c4 += 4)
-                        __stcs(reinterpret_cast<uint4*>(o + c4), make_uint4(own_col, own_col, own_col, own_col));
-                } else {
-                    for (int c = 0; c < s; c++) o[c] = own_col;
-                }
-            }
+        if (!full || intr) {
+            // owner resolution after the barrier, over a compacted list, so
+            // that warps do not run it beside blocks that need none
+            M.list[atomicAdd(&M.slow, 1)] = (uint16_t)q;
             continue;
         }
+        const uint32_t own_col = rgba_of(M.pix[ty + 2][tx + 2]);
+        uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
+        for (int r = 0; r < s; r++) {
+            uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
+            if (vec) {
+                for (int c4 = 0; c4 < s; c4 += 4)
+                    __stcs(reinterpret_cast<uint4*>(o + c4), make_uint4(own_col, own_col, own_col, own_col));
+            } else {
+                for (int c = 0; c < s; c++) o[c] = own_col;
+            }
+        }
+    }
+    __syncthreads();
+    const int nslow = M.slow;
+    for (int qs = threadIdx.x; qs < nslow; qs += blockDim.x) {
+        const int q = M.list[qs];
+        const int tx = q % TW, ty = q / TW;
+        const int ci = x0 + tx, cj = y0 + ty;
+        const int k0 = (ty + 1) * T::GW + (tx + 1);
+        uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
         for (int r = 0; r < s; r++) {
             // per candidate (priority order q = 0..8: rows above first, then
             // right to left) the samples of this row it covers and no
