@@ -886,6 +886,10 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         const int ci = x0 + tx, cj = y0 + ty;
         const int k0 = (ty + 1) * T::GW + (tx + 1);
         uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
+        // the nine candidates' colours, in priority order
+        uint32_t cand_col[9];
+#pragma unroll
+        for (int z = 0; z < 9; z++) cand_col[z] = rgba_of(M.pix[ty + 2 + 1 - z / 3][tx + 2 + 1 - z % 3]);
         for (int r = 0; r < s; r++) {
             // per candidate (priority order q = 0..8: rows above first, then
             // right to left) the samples of this row it covers and no
@@ -913,13 +917,11 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             }
             uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
             auto owner_colour = [&](int c) -> uint32_t {
-                if (!((claimed >> c) & 1u)) return 0xFF000000u;
-                int z = 0;
+                uint32_t col = 0xFF000000u; // no owner: the clear colour
 #pragma unroll
                 for (int q = 0; q < 9; q++)
-                    if ((take[q] >> c) & 1u) z = q;
-                // candidate z is the cell (di, dj) = (1 - z % 3, 1 - z / 3)
-                return rgba_of(M.pix[ty + 2 + 1 - z / 3][tx + 2 + 1 - z % 3]);
+                    if ((take[q] >> c) & 1u) col = cand_col[q];
+                return col;
             };
             if (vec) {
 #pragma unroll
