@@ -619,6 +619,10 @@ cudaError_t build_scale_masks(int s, uint32_t* lut, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// slots of a tile's table of distinct cut polygons (bounded probing: a
+// polygon that finds no slot makes its own mask)
+constexpr int kPolyTable = 1024, kPolyProbes = 16;
+
 template <int TW, int TH>
 struct MaskTile {
     static constexpr int GW = TW + 2, GH = TH + 2, GN = GW * GH; // cells with their ring
@@ -629,8 +633,12 @@ struct MaskTile {
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
     uint8_t live[GN];  // the cell exists (inside the image)
     uint16_t list[GN]; // subdivided cells of the tile, then the blocks that need owner resolution
+    uint16_t rep[GN];  // per subdivided cell: the list entry whose polygon (and mask) it shares
+    uint16_t reps[GN]; // list entries that make a mask
+    unsigned long long table[kPolyTable]; // distinct polygons: hash tag | (list entry + 1), 0 empty
     int count;
     int slow;          // blocks in list for the owner-resolution pass
+    int nreps;
 };
 
 __device__ __forceinline__ uint32_t rgba_of(uint32_t p)
@@ -734,9 +742,11 @@ __device__ __noinline__ int ear_clip_mask(const Packed& P, int u, int mlo, int F
 // subdivided cell. G(dx, dy) is the graph byte of the cell at that offset
 // (0 outside the image, bits toward outside cleared); TJ(px, py) the corner
 // test.
+// The cut polygon of a subdivided cell (G(dx, dy): graph byte of the cell at
+// that offset, 0 outside the image, bits toward outside cleared; TJ(px, py):
+// the corner test).
 template <typename GraphAt, typename TJ>
-__device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const MaskGeom& Gm, uint32_t* rows,
-                                                      int rstride)
+__device__ __forceinline__ void cell_polygon(GraphAt G, TJ tj, Packed& sp)
 {
     const unsigned node = G(0, 0);
     const int pat = cell_pattern(node, G(-1, 0), G(1, 0));
@@ -745,8 +755,13 @@ __device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const Ma
         const int dx = dir_di(L), dy = dir_dj(L);
         return cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy));
     };
-    Packed sp;
     subdivide_tables(pat, e, nb_pattern, tj, sp);
+}
+
+// Coverage rows of a cut polygon and its spill bits (0 when the ear clip
+// gives up, as the reference then draws nothing for the cell).
+__device__ __forceinline__ unsigned polygon_mask(const Packed& sp, const MaskGeom& Gm, uint32_t* rows, int rstride)
+{
     for (int r = 0; r < Gm.F; r++) rows[r * rstride] = 0;
     const int u = 4 * Gm.s;
     int mnx, mny, mxx, mxy;
@@ -757,6 +772,38 @@ __device__ __forceinline__ unsigned complex_cell_mask(GraphAt G, TJ tj, const Ma
         if (ear_clip_mask(sp, u, Gm.mlo, Gm.F, rows, rstride) == 0) return 0;
     }
     return spill_bits(mnx, mny, mxx, mxy);
+}
+
+// A cut polygon parked in its own cell's mask rows (10 words) until the mask
+// is made, and a 64-bit mix of it for the tile's table of distinct polygons.
+__device__ __forceinline__ void park_polygon(const Packed& sp, uint32_t* rows)
+{
+    rows[0] = (uint32_t)sp.x0; rows[1] = (uint32_t)(sp.x0 >> 32);
+    rows[2] = (uint32_t)sp.x1; rows[3] = (uint32_t)(sp.x1 >> 32);
+    rows[4] = (uint32_t)sp.y0; rows[5] = (uint32_t)(sp.y0 >> 32);
+    rows[6] = (uint32_t)sp.y1; rows[7] = (uint32_t)(sp.y1 >> 32);
+    rows[8] = (uint32_t)sp.n;
+}
+
+__device__ __forceinline__ void unpark_polygon(const uint32_t* rows, Packed& sp)
+{
+    sp.x0 = rows[0] | (uint64_t)rows[1] << 32;
+    sp.x1 = rows[2] | (uint64_t)rows[3] << 32;
+    sp.y0 = rows[4] | (uint64_t)rows[5] << 32;
+    sp.y1 = rows[6] | (uint64_t)rows[7] << 32;
+    sp.n = (int)rows[8];
+}
+
+__device__ __forceinline__ uint64_t polygon_hash(const Packed& sp)
+{
+    uint64_t h = sp.x0 ^ (sp.x1 * 0x9E3779B97F4A7C15ull) ^ ((sp.y0 << 1 | sp.y0 >> 63) * 0xC2B2AE3D27D4EB4Full) ^
+                 ((sp.y1 << 7 | sp.y1 >> 57) * 0x165667B19E3779F9ull) ^ (uint64_t)sp.n;
+    h ^= h >> 33;
+    h *= 0xFF51AFD7ED558CCDull;
+    h ^= h >> 33;
+    h *= 0xC4CEB9FE1A85EC53ull;
+    h ^= h >> 33;
+    return h;
 }
 
 template <int LAYOUT, int S, int TW, int TH>
@@ -772,7 +819,9 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
     if (threadIdx.x == 0) {
         M.count = 0;
         M.slow = 0;
+        M.nreps = 0;
     }
+    for (int k = threadIdx.x; k < kPolyTable; k += blockDim.x) M.table[k] = 0ull;
     for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
         int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
         unsigned v = 0;
@@ -838,9 +887,64 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
             return false;
         };
-        M.spill[k] = (uint8_t)complex_cell_mask(Gs, tj, G, masks + (size_t)k * F, 1);
+        Packed sp;
+        cell_polygon(Gs, tj, sp);
+        uint32_t* rows = masks + (size_t)k * F;
+        if (F < 10) { // no room to park the polygon: every cell makes its mask
+            M.spill[k] = (uint8_t)polygon_mask(sp, G, rows, 1);
+            continue;
+        }
+        // the mask depends on the polygon alone: one cell per distinct polygon
+        // of the tile makes it, the others copy
+        park_polygon(sp, rows);
+        __threadfence_block();
+        const uint64_t h = polygon_hash(sp);
+        const unsigned long long tag = h & ~0xFFFFull;
+        int slot = (int)(h >> 16) & (kPolyTable - 1), rep = -1;
+        for (int probe = 0; probe < kPolyProbes && rep < 0; probe++, slot = (slot + 1) & (kPolyTable - 1)) {
+            unsigned long long cur = M.table[slot];
+            if (cur == 0ull) {
+                cur = atomicCAS(&M.table[slot], 0ull, tag | (unsigned long long)(q + 1));
+                if (cur == 0ull) {
+                    rep = q;
+                    break;
+                }
+            }
+            if ((cur & ~0xFFFFull) == tag) {
+                const int rq = (int)(cur & 0xFFFFull) - 1;
+                Packed other;
+                unpark_polygon(masks + (size_t)M.list[rq] * F, other);
+                if (other.n == sp.n && other.x0 == sp.x0 && other.x1 == sp.x1 && other.y0 == sp.y0 &&
+                    other.y1 == sp.y1)
+                    rep = rq;
+            }
+        }
+        if (rep < 0) rep = q;
+        M.rep[q] = (uint16_t)rep;
+        if (rep == q) M.reps[atomicAdd(&M.nreps, 1)] = (uint16_t)q;
     }
     __syncthreads();
+    if (F >= 10) {
+        const int nreps = M.nreps;
+        for (int i = threadIdx.x; i < nreps; i += blockDim.x) {
+            const int k = M.list[M.reps[i]];
+            uint32_t* rows = masks + (size_t)k * F;
+            Packed sp;
+            unpark_polygon(rows, sp);
+            M.spill[k] = (uint8_t)polygon_mask(sp, G, rows, 1);
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
+            const int rq = M.rep[q];
+            if (rq == q) continue;
+            const int k = M.list[q], rk = M.list[rq];
+            const uint32_t* src = masks + (size_t)rk * F;
+            uint32_t* dst = masks + (size_t)k * F;
+            for (int r = 0; r < F; r++) dst[r] = src[r];
+            M.spill[k] = M.spill[rk];
+        }
+        __syncthreads();
+    }
 
     // ---- phase C: one output block per tile cell
     const int ow = w * s;
