@@ -194,23 +194,35 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
         }
         *reinterpret_cast<uint32_t*>(&s[ry][rx]) = v;
     }
-    __syncthreads();
     SnapTile t{s, ox, oy};
+    // each 2x2 block touching the tile decided once (the four corner nodes
+    // each clear their own bit of it): bit 0 a crossing, bit 1 the decision
+    // (true removes "/", false "\"); blocks reaching outside the image read
+    // the zero halo and are never crossings
+    __shared__ uint8_t dec[kHTH + 1][kHTW + 1];
+    __syncthreads();
+    for (int k = threadIdx.x; k < (kHTW + 1) * (kHTH + 1); k += blockDim.x) {
+        const int bx = k % (kHTW + 1), by = k / (kHTW + 1);
+        const int bi = x0 - 1 + bx, bj = y0 - 1 + by;
+        uint8_t d = 0;
+        if (bitof(t.at(bi, bj), 2) && bitof(t.at(bi, bj + 1), 7) && bitof(t.at(bi + 1, bj), 0) &&
+            bitof(t.at(bi + 1, bj + 1), 5))
+            d = 1 | (block_decision(t, bi, bj) ? 2 : 0);
+        dec[by][bx] = d;
+    }
+    __syncthreads();
     for (int k = threadIdx.x; k < kHTW * kHTH; k += blockDim.x) {
-        int i = x0 + k % kHTW, j = y0 + k / kHTW;
+        const int tx = k % kHTW, ty = k / kHTW;
+        const int i = x0 + tx, j = y0 + ty;
         if (i >= w || j >= h) continue;
-        unsigned c = t.at(i, j), o = c;
-        // only nodes with a diagonal can be touched
-        if (c & 0xA5u) {
-            if (bitof(t.at(i - 1, j), 2) && bitof(t.at(i - 1, j + 1), 7) && bitof(c, 0) && bitof(t.at(i, j + 1), 5))
-                if (!block_decision(t, i - 1, j)) o &= ~1u;
-            if (bitof(t.at(i - 1, j - 1), 2) && bitof(t.at(i - 1, j), 7) && bitof(t.at(i, j - 1), 0) && bitof(c, 5))
-                if (block_decision(t, i - 1, j - 1)) o &= ~32u;
-            if (bitof(t.at(i, j - 1), 2) && bitof(c, 7) && bitof(t.at(i + 1, j - 1), 0) && bitof(t.at(i + 1, j), 5))
-                if (!block_decision(t, i, j - 1)) o &= ~128u;
-            if (bitof(c, 2) && bitof(t.at(i, j + 1), 7) && bitof(t.at(i + 1, j), 0) && bitof(t.at(i + 1, j + 1), 5))
-                if (block_decision(t, i, j)) o &= ~4u;
-        }
+        unsigned o = t.at(i, j);
+        // the node is the lower-right corner of block (i-1, j), the upper-right
+        // of (i-1, j-1), the upper-left of (i, j-1), the lower-left of (i, j)
+        const unsigned a = dec[ty + 1][tx], b = dec[ty][tx], c = dec[ty][tx + 1], d = dec[ty + 1][tx + 1];
+        if (a == 1) o &= ~1u;
+        if (b == 3) o &= ~32u;
+        if (c == 1) o &= ~128u;
+        if (d == 3) o &= ~4u;
         out[(size_t)j * w + i] = (uint8_t)o;
     }
 }
