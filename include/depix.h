@@ -218,7 +218,8 @@ depix_status depix_context_launch_shape(depix_context* ctx, int* gran, int* tile
 enum {
     DEPIX_STAGE_GRAPH = 0,      /* similarity graph + trivial removal */
     DEPIX_STAGE_HEURISTICS = 1, /* heuristic crossing resolution */
-    DEPIX_STAGE_LABELS = 2,     /* component labels */
+    DEPIX_STAGE_LABELS = 2,     /* component labels: merge across tiles and flatten (with labels on, the
+                                   heuristics stage also makes each tile's local labels) */
     DEPIX_STAGE_RASTER = 3,     /* cells, subdivision, coverage masks, block resolution, output */
     DEPIX_STAGE_COUNT = 4
 };

@@ -481,13 +481,15 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
             DEPIX_CK(launch_graph(gb, n, thr, true, s));
         }
         {
+            // with labels, each heuristics tile also makes its local labels
             StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
             GraphBatch hb{ctx->graph_a, ctx->graph_b, px, w[0], h[0]};
-            DEPIX_CK(launch_heuristics(hb, n, s));
+            if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, n, d_labels, s));
+            else DEPIX_CK(launch_heuristics(hb, n, s));
         }
         if (d_labels) {
-            StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
-            DEPIX_CK(launch_labels(ctx->graph_b, d_labels, w[0], h[0], n, px, s));
+            StageTimer t(ctx, DEPIX_STAGE_LABELS, 2, s);
+            DEPIX_CK(launch_labels_after_heuristics(ctx->graph_b, d_labels, w[0], h[0], n, px, s));
         }
         {
             RasterBatch rb{img0, (size_t)is, ctx->graph_b, px, d_out + out_offset[0], (size_t)os, w[0], h[0],
@@ -514,7 +516,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
                                              DEPIX_STAGE_RASTER};
         for (int st = 0; st < QS_COUNT; st++) {
             if (st == QS_LABEL && !d_labels) continue;
-            StageTimer t(ctx, kStage[st], st == QS_LABEL ? 3 : 1, s);
+            StageTimer t(ctx, kStage[st], st == QS_LABEL ? 2 : 1, s);
             DEPIX_TRY(queue_launch_stage(ctx->queue, st, s));
         }
         return DEPIX_OK;
@@ -532,11 +534,12 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         {
             StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
             GraphBatch hb{ctx->graph_a + goff, ctx->graph_b + goff, 0, w[k], h[k]};
-            DEPIX_CK(launch_heuristics(hb, 1, s));
+            if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, 1, d_labels + loff, s));
+            else DEPIX_CK(launch_heuristics(hb, 1, s));
         }
         if (d_labels) {
-            StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
-            DEPIX_CK(launch_labels(ctx->graph_b + goff, d_labels + loff, w[k], h[k], 1, 0, s));
+            StageTimer t(ctx, DEPIX_STAGE_LABELS, 2, s);
+            DEPIX_CK(launch_labels_after_heuristics(ctx->graph_b + goff, d_labels + loff, w[k], h[k], 1, 0, s));
         }
         {
             RasterBatch rb{img, 0, ctx->graph_b + goff, 0, d_out + out_offset[k], 0, w[k], h[k], 4 * w[k],
@@ -748,11 +751,12 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
     {
         StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
         GraphBatch hb{ctx->graph_a, resolved, 0, w, h};
-        DEPIX_CK(launch_heuristics(hb, 1, s));
+        if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, 1, d_labels, s));
+        else DEPIX_CK(launch_heuristics(hb, 1, s));
     }
     if (d_labels) {
-        StageTimer t(ctx, DEPIX_STAGE_LABELS, 3, s);
-        DEPIX_CK(launch_labels(resolved, d_labels, w, h, 1, 0, s));
+        StageTimer t(ctx, DEPIX_STAGE_LABELS, 2, s);
+        DEPIX_CK(launch_labels_after_heuristics(resolved, d_labels, w, h, 1, 0, s));
     }
     if (d_out) {
         RasterBatch rb{d_img, 0, resolved, 0, d_out, 0, w, h, widthstep, (int)layout, p->scale, p->subdivide};

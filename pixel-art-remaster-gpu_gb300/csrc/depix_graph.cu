@@ -174,7 +174,15 @@ __device__ bool block_decision(const SnapTile& t, int i, int j)
     return !(seg2 < seg);
 }
 
-__device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* out, int w, int h, int x0, int y0)
+template <int TW, int TH>
+__device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t* L, int w, int h, int x0, int y0);
+
+// Heuristic resolution of one 64x16 tile; with L set, the tile's local
+// component labels too (union-find over the resolved bytes, still in shared
+// memory), which leaves the label stage only the merge across tile borders
+// and the flattening.
+__device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* out, int w, int h, int x0, int y0,
+                                                int32_t* L = nullptr)
 {
     __shared__ __align__(16) uint8_t s[kHRH][kHRW];
     const int ox = x0 - kHalo, oy = y0 - kHalo;
@@ -211,10 +219,14 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
         dec[by][bx] = d;
     }
     __syncthreads();
+    __shared__ uint8_t res[kHTW * kHTH];
     for (int k = threadIdx.x; k < kHTW * kHTH; k += blockDim.x) {
         const int tx = k % kHTW, ty = k / kHTW;
         const int i = x0 + tx, j = y0 + ty;
-        if (i >= w || j >= h) continue;
+        if (i >= w || j >= h) {
+            res[k] = 0;
+            continue;
+        }
         unsigned o = t.at(i, j);
         // the node is the lower-right corner of block (i-1, j), the upper-right
         // of (i-1, j-1), the upper-left of (i, j-1), the lower-left of (i, j)
@@ -224,6 +236,13 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
         if (c == 1) o &= ~128u;
         if (d == 3) o &= ~4u;
         out[(size_t)j * w + i] = (uint8_t)o;
+        res[k] = (uint8_t)(o & inside_mask(i, j, w, h));
+    }
+    if (L) {
+        __shared__ int sl[kHTW * kHTH];
+        __shared__ uint16_t run[kHTW * kHTH];
+        __syncthreads();
+        cc_local_core<kHTW, kHTH>(res, sl, run, L, w, h, x0, y0);
     }
 }
 
@@ -232,6 +251,13 @@ __global__ void __launch_bounds__(256) k_heuristics(GraphBatch b)
     const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
     uint8_t* out = b.out + b.frame_stride * blockIdx.z;
     heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH);
+}
+
+__global__ void __launch_bounds__(256) k_heuristics_labels(GraphBatch b, int32_t* L)
+{
+    const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
+    uint8_t* out = b.out + b.frame_stride * blockIdx.z;
+    heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH, L + b.frame_stride * blockIdx.z);
 }
 
 // -------------------------------------------------- component labelling
@@ -304,7 +330,60 @@ __device__ __forceinline__ void s_unite(int* L, int a, int b)
     }
 }
 
-// union-find inside one 32x32 tile (x0, y0): local roots as global indices
+// Union-find over a TW x TH tile whose graph bytes are in shared memory (sg,
+// row-major, 0 outside the image): local roots as global indices. A warp
+// owns a row and walks its 32-pixel segments left to right: horizontal runs
+// from one ballot per segment (a run's root is its leftmost pixel, carried
+// across segments), rows joined with one union per pair of touching runs.
+template <int TW, int TH>
+__device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t* L, int w, int h, int x0, int y0)
+{
+    static_assert(TW % 32 == 0 && TW * TH <= 65536, "tile shape");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int r = warp; r < TH; r += nwarp) {
+        int carry = r * TW;
+#pragma unroll
+        for (int sgm = 0; sgm < TW / 32; sgm++) {
+            const int c = sgm * 32 + lane, p = r * TW + c;
+            const bool link = c > 0 && (bitof(sg[p], 3) || bitof(sg[p - 1], 4));
+            const unsigned starts = __ballot_sync(0xFFFFFFFFu, !link);
+            const unsigned upto = lane == 31 ? starts : (starts & ((2u << lane) - 1u));
+            const int root = upto ? r * TW + sgm * 32 + (31 - __clz(upto)) : carry;
+            run[p] = (uint16_t)root;
+            sl[p] = root;
+            carry = __shfl_sync(0xFFFFFFFFu, root, 31);
+        }
+    }
+    __syncthreads();
+    for (int r = warp; r < TH - 1; r += nwarp) {
+#pragma unroll
+        for (int sgm = 0; sgm < TW / 32; sgm++) {
+            const int c = sgm * 32 + lane, p = r * TW + c;
+            const unsigned node = sg[p];
+#pragma unroll
+            for (int e = 0; e <= 2; e++) { // up-left, up, up-right
+                const int nc = c + dir_di(e);
+                if (nc < 0 || nc >= TW) continue;
+                const int q = p + TW + dir_di(e);
+                if (!(bitof(node, e) || bitof(sg[q], 7 - e))) continue;
+                // the pixel to the left already joins the same two runs
+                if (c > 0 && nc > 0 && run[p - 1] == run[p] && run[q - 1] == run[q] &&
+                    (bitof(sg[p - 1], e) || bitof(sg[q - 1], 7 - e)))
+                    continue;
+                s_unite(sl, run[p], run[q]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < TW * TH; p += blockDim.x) {
+        const int x = x0 + p % TW, y = y0 + p / TW;
+        if (x >= w || y >= h) continue;
+        const int r = s_find(sl, p);
+        L[(size_t)y * w + x] = (y0 + r / TW) * w + (x0 + r % TW);
+    }
+}
+
+// union-find inside one 32x32 tile (x0, y0) of a graph in global memory
 __device__ void cc_local_tile(const uint8_t* g, int32_t* L, int w, int h, int x0, int y0)
 {
     __shared__ int sl[kLT * kLT];
@@ -315,40 +394,7 @@ __device__ void cc_local_tile(const uint8_t* g, int32_t* L, int w, int h, int x0
         sg[p] = (x < w && y < h) ? g[(size_t)y * w + x] & inside_mask(x, y, w, h) : 0;
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int r = warp; r < kLT; r += nwarp) {
-        int p = r * kLT + lane;
-        bool link = lane > 0 && (bitof(sg[p], 3) || bitof(sg[p - 1], 4));
-        unsigned starts = __ballot_sync(0xFFFFFFFFu, !link);
-        unsigned upto = lane == 31 ? starts : (starts & ((2u << lane) - 1u));
-        int root = r * kLT + (31 - __clz(upto));
-        run[p] = (uint16_t)root;
-        sl[p] = root;
-    }
-    __syncthreads();
-    for (int r = warp; r < kLT - 1; r += nwarp) {
-        int p = r * kLT + lane;
-        unsigned node = sg[p];
-#pragma unroll
-        for (int e = 0; e <= 2; e++) { // up-left, up, up-right
-            int nl = lane + dir_di(e);
-            if (nl < 0 || nl >= kLT) continue;
-            int q = p + kLT + dir_di(e);
-            if (!(bitof(node, e) || bitof(sg[q], 7 - e))) continue;
-            // the lane to the left already joins the same two runs
-            if (lane > 0 && nl > 0 && run[p - 1] == run[p] && run[q - 1] == run[q] &&
-                (bitof(sg[p - 1], e) || bitof(sg[q - 1], 7 - e)))
-                continue;
-            s_unite(sl, run[p], run[q]);
-        }
-    }
-    __syncthreads();
-    for (int p = threadIdx.x; p < kLT * kLT; p += blockDim.x) {
-        int x = x0 + p % kLT, y = y0 + p / kLT;
-        if (x >= w || y >= h) continue;
-        int r = s_find(sl, p);
-        L[(size_t)y * w + x] = (y0 + r / kLT) * w + (x0 + r % kLT);
-    }
+    cc_local_core<kLT, kLT>(sg, sl, run, L, w, h, x0, y0);
 }
 
 __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
@@ -362,17 +408,19 @@ __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, 
 // harmless). One thread per border pixel of a tile (4 * 32 - 4 of them).
 constexpr int kLBorder = 4 * kLT - 4;
 
-// unions of border pixel q of tile `tile` with neighbours in other tiles
-__device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
+// unions of border pixel q (of 2 TW + 2 (TH - 2)) of tile `tile` in a TW x TH
+// tiling with neighbours in other tiles
+template <int TW, int TH>
+__device__ __forceinline__ void cc_merge_border_t(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
 {
-    const int tiles_x = (w + kLT - 1) / kLT;
+    const int tiles_x = (w + TW - 1) / TW;
     // border position q: bottom row, top row, then left and right columns
     int lx, ly;
-    if (q < kLT) { lx = q; ly = 0; }
-    else if (q < 2 * kLT) { lx = q - kLT; ly = kLT - 1; }
-    else if (q < 3 * kLT - 2) { lx = 0; ly = q - 2 * kLT + 1; }
-    else { lx = kLT - 1; ly = q - (3 * kLT - 2) + 1; }
-    const int i = (tile % tiles_x) * kLT + lx, j = (tile / tiles_x) * kLT + ly;
+    if (q < TW) { lx = q; ly = 0; }
+    else if (q < 2 * TW) { lx = q - TW; ly = TH - 1; }
+    else if (q < 2 * TW + TH - 2) { lx = 0; ly = q - 2 * TW + 1; }
+    else { lx = TW - 1; ly = q - (2 * TW + TH - 2) + 1; }
+    const int i = (tile % tiles_x) * TW + lx, j = (tile / tiles_x) * TH + ly;
     if (i >= w || j >= h) return;
     const int k = j * w + i;
     unsigned node = g[k];
@@ -381,9 +429,26 @@ __device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, in
         if (!bitof(node, e)) continue;
         int ni = i + dir_di(e), nj = j + dir_dj(e);
         if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
-        if (ni / kLT == i / kLT && nj / kLT == j / kLT) continue;
+        if (ni / TW == i / TW && nj / TH == j / TH) continue;
         uf_unite(L, k, nj * w + ni);
     }
+}
+
+__device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
+{
+    cc_merge_border_t<kLT, kLT>(g, L, w, h, tile, q);
+}
+
+// border pixels of a 64x16 tile: the merge after the fused local labels
+constexpr int kHBorder = 2 * kHTW + 2 * (kHTH - 2);
+
+__global__ void k_cc_merge_h(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
+    if (t / kHBorder >= tiles) return;
+    cc_merge_border_t<kHTW, kHTH>(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, t / kHBorder,
+                                  t % kHBorder);
 }
 
 __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
@@ -428,33 +493,23 @@ __global__ void __launch_bounds__(256) k_heur_queue(QueueBatch q)
         const QueueFrame fr = H->frames[f];
         const int lt = t - (int)base[f], tx = (fr.w + kHTW - 1) / kHTW;
         heuristics_tile(q.graph_a + fr.px_off, q.graph_b + fr.px_off, fr.w, fr.h, (lt % tx) * kHTW,
-                        (lt / tx) * kHTH);
+                        (lt / tx) * kHTH, H->labels ? H->labels + fr.px_off : nullptr);
     });
 }
 
-__global__ void __launch_bounds__(256) k_label_local_queue(QueueBatch q)
-{
-    const QueueHeader* H = q.hdr;
-    const int n = H->n;
-    queue_loop(q.counters + QC_LOCAL, (int)H->total[QS_LABEL], q.gran[QS_LABEL], [&](int t) {
-        const uint32_t* base = H->base + QS_LABEL * (n + 1);
-        const int f = queue_frame(base, n, (uint32_t)t);
-        const QueueFrame fr = H->frames[f];
-        const int lt = t - (int)base[f], tx = (fr.w + kLT - 1) / kLT;
-        cc_local_tile(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h, (lt % tx) * kLT, (lt / tx) * kLT);
-    });
-}
 
 __global__ void __launch_bounds__(128) k_label_merge_queue(QueueBatch q)
 {
+    // the local labels came with the heuristics stage: its tiles, its prefix
     const QueueHeader* H = q.hdr;
     const int n = H->n;
-    queue_loop(q.counters + QC_MERGE, (int)H->total[QS_LABEL], q.gran[QS_LABEL], [&](int t) {
-        const uint32_t* base = H->base + QS_LABEL * (n + 1);
+    queue_loop(q.counters + QC_MERGE, (int)H->total[QS_HEUR], q.gran[QS_LABEL], [&](int t) {
+        const uint32_t* base = H->base + QS_HEUR * (n + 1);
         const int f = queue_frame(base, n, (uint32_t)t);
         const QueueFrame fr = H->frames[f];
-        for (int b = threadIdx.x; b < kLBorder; b += blockDim.x)
-            cc_merge_border(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h, t - (int)base[f], b);
+        for (int b = threadIdx.x; b < kHBorder; b += blockDim.x)
+            cc_merge_border_t<kHTW, kHTH>(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h,
+                                          t - (int)base[f], b);
     });
 }
 
@@ -490,7 +545,7 @@ cudaError_t queue_heuristics(const QueueBatch& q, int blocks, cudaStream_t s)
 
 cudaError_t queue_labels(const QueueBatch& q, int blocks, cudaStream_t s)
 {
-    k_label_local_queue<<<blocks, 256, 0, s>>>(q);
+    // local labels were made by the heuristics stage
     k_label_merge_queue<<<blocks, 128, 0, s>>>(q);
     k_label_flatten_queue<<<blocks, 256, 0, s>>>(q);
     return cudaGetLastError();
@@ -513,7 +568,7 @@ int queue_blocks_per_sm(int stage, const QueueBatch& q)
     switch (stage) {
     case QS_GRAPH: return occupancy(k_graph_queue, 256);
     case QS_HEUR: return occupancy(k_heur_queue, 256);
-    case QS_LABEL: return std::min(occupancy(k_label_local_queue, 256), occupancy(k_label_flatten_queue, 256));
+    case QS_LABEL: return occupancy(k_label_flatten_queue, 256);
     default: return queue_raster_blocks_per_sm(q);
     }
 }
@@ -555,6 +610,24 @@ cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s)
 {
     dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
     k_heuristics<<<grid, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_heuristics_labels(const GraphBatch& b, int nframes, int32_t* labels, cudaStream_t s)
+{
+    dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
+    k_heuristics_labels<<<grid, 256, 0, s>>>(b, labels);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, int w, int h, int nframes,
+                                          size_t frame_stride, cudaStream_t s)
+{
+    const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
+    const int borders = tiles * kHBorder;
+    k_cc_merge_h<<<dim3((borders + 127) / 128, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
+    const int n = w * h;
+    k_cc_flatten<<<dim3((n + 255) / 256, 1, nframes), 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }
 

@@ -156,6 +156,11 @@ void set_last_error(const std::string& msg);
 cudaError_t launch_graph(const FrameBatch& b, int nframes, uint32_t thr, bool fuse_trivial, cudaStream_t s);
 cudaError_t launch_trivial(uint8_t* g, int w, int h, cudaStream_t s);
 cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s);
+// heuristics with each tile's local component labels fused in, then the
+// label stage's remainder (merge across the 64x16 tile borders, flatten)
+cudaError_t launch_heuristics_labels(const GraphBatch& b, int nframes, int32_t* labels, cudaStream_t s);
+cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, int w, int h, int nframes,
+                                          size_t frame_stride, cudaStream_t s);
 cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int nframes, size_t frame_stride,
                           cudaStream_t s);
 
