@@ -13,7 +13,7 @@ namespace depix {
 // right (bit 0), upper (bit 1), upper-right (bit 2) pixel, and of the pair
 // (right, upper) (bit 3), each only when both pixels are in the image.
 constexpr int kGTW = 64;  // graph tile width (pixels)
-constexpr int kGTH = 8;   // graph tile height
+constexpr int kGTH = 16;  // graph tile height
 
 template <int LAYOUT>
 __device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uint32_t thr, bool fuse_trivial)
@@ -46,8 +46,18 @@ __device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uin
         pairs[ry][rx] = (uint8_t)pb;
     }
     __syncthreads();
-    // node bits (graph_Kernel) and, fused, the trivial removal (crossCheck_4):
-    // a diagonal goes when the 2x2 block it crosses has all four sides similar
+    // fused trivial removal (crossCheck_4): a diagonal goes when the 2x2 block
+    // it crosses has all four sides similar; each block decided once (bit 4
+    // of the pairs byte of its lower-left node)
+    if (fuse_trivial) {
+        for (int k = threadIdx.x; k < (kGTW + 1) * (kGTH + 1); k += blockDim.x) {
+            const int bx = k % (kGTW + 1), by = k / (kGTW + 1);
+            const unsigned full = pairs[by][bx] & pairs[by + 1][bx] & (pairs[by][bx] >> 1) & (pairs[by][bx + 1] >> 1) & 1u;
+            pairs[by][bx] |= (uint8_t)(full << 4);
+        }
+        __syncthreads();
+    }
+    // node bits (graph_Kernel)
     for (int k = threadIdx.x; k < kGTW * kGTH; k += blockDim.x) {
         int tx = k % kGTW, ty = k / kGTW;
         int gx = x0 + tx, gy = y0 + ty;
@@ -64,15 +74,11 @@ __device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uin
         node |= (unsigned)bitof(dl, 2) << 5;  // down-left
         node |= (unsigned)bitof(d, 3) << 7;   // down-right: pair (right of d, up of d = c)
         if (fuse_trivial) {
-            // block with lower-left (bx, by) full: H(bx,by) H(bx,by+1) V(bx,by) V(bx+1,by)
-            auto full = [&](int bx, int by) {
-                return bitof(pairs[by][bx], 0) && bitof(pairs[by + 1][bx], 0) && bitof(pairs[by][bx], 1) &&
-                       bitof(pairs[by][bx + 1], 1);
-            };
-            if (full(rx, ry)) node &= ~4u;
-            if (full(rx - 1, ry)) node &= ~1u;
-            if (full(rx - 1, ry - 1)) node &= ~32u;
-            if (full(rx, ry - 1)) node &= ~128u;
+            // blocks with lower-left (rx, ry), (rx-1, ry), (rx-1, ry-1), (rx, ry-1)
+            if (bitof(c, 4)) node &= ~4u;
+            if (bitof(l, 4)) node &= ~1u;
+            if (bitof(dl, 4)) node &= ~32u;
+            if (bitof(d, 4)) node &= ~128u;
         }
         f.graph[(size_t)gy * w + gx] = (uint8_t)node;
     }

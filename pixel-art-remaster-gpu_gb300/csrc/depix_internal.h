@@ -97,7 +97,7 @@ struct QueueBatch {
 // tiles of a frame per stage; the raster has three tile shapes, each with its
 // own prefix (QS_RASTER + shape index), so a batch can be raster-timed in
 // every shape without new descriptors
-constexpr int kQGraphTW = 64, kQGraphTH = 8, kQHeurTW = 64, kQHeurTH = 16, kQLabelT = 32;
+constexpr int kQGraphTW = 64, kQGraphTH = 16, kQHeurTW = 64, kQHeurTH = 16, kQLabelT = 32;
 constexpr int kQRasterShapes = 3;
 constexpr int kQPrefixes = QS_RASTER + kQRasterShapes;
 static_assert(kQPrefixes == 6, "QueueHeader::total");
