@@ -206,7 +206,8 @@ depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int
 
 /* Launch shape of the queue path (uneven batches): tiles pulled per queue
  * step, 1, 2, 4 or 8 (0: tuned, the default), and the raster tile in cells,
- * 32x32, 32x16 or 16x16. Tuning runs on the first batch of each bucket of
+ * 32x32, 32x16, 16x16, or 0x0: each frame in the shape with the fewest cells
+ * to process (one raster launch per shape). Tuning runs on the first batch of each bucket of
  * frame count and mean frame size (powers of two), scale and label choice, by
  * timing the candidate shapes on that batch (it synchronises the stream). */
 depix_status depix_context_set_launch_shape(depix_context* ctx, int gran, int tile_w, int tile_h);

@@ -679,8 +679,9 @@ depix_status depix_context_set_launch_shape(depix_context* c, int gran, int tile
         return DEPIX_OK;
     }
     if (gran != 1 && gran != 2 && gran != 4 && gran != 8) return arg_fail("granularity must be 0, 1, 2, 4 or 8");
-    if (!((tile_w == 32 && tile_h == 32) || (tile_w == 32 && tile_h == 16) || (tile_w == 16 && tile_h == 16)))
-        return arg_fail("raster tile must be 32x32, 32x16 or 16x16");
+    if (!((tile_w == 32 && tile_h == 32) || (tile_w == 32 && tile_h == 16) || (tile_w == 16 && tile_h == 16) ||
+          (tile_w == 0 && tile_h == 0)))
+        return arg_fail("raster tile must be 32x32, 32x16, 16x16 or 0x0 (each frame its own)");
     c->shape = QueueShape{{gran, gran, gran, gran}, tile_w, tile_h};
     c->shape_forced = true;
     return DEPIX_OK;

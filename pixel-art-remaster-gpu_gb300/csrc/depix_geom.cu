@@ -1077,8 +1077,9 @@ __global__ void __launch_bounds__(256, 3) k_raster_queue(QueueBatch q)
     extern __shared__ uint32_t masks[];
     const QueueHeader* H = q.hdr;
     const int n = H->n;
-    queue_loop(q.counters + QC_RASTER, (int)H->total[QS_RASTER + raster_shape_index(TW, TH)], q.gran[QS_RASTER], [&](int t) {
-        constexpr int P = QS_RASTER + raster_shape_index(TW, TH);
+    constexpr int SH = raster_shape_index(TW, TH);
+    const int P = q.rbase + SH;
+    queue_loop(q.counters + QC_RASTER + SH, (int)H->total[P], q.gran[QS_RASTER], [&](int t) {
         const uint32_t* base = H->base + P * (n + 1);
         const int f = queue_frame(base, n, (uint32_t)t);
         const QueueFrame fr = H->frames[f];

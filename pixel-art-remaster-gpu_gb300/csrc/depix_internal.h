@@ -57,7 +57,8 @@ struct RasterBatch {
 // memory; persistent kernels pull tile indices from a counter and find a
 // tile's frame by binary search over the prefix.
 enum QueueStage { QS_GRAPH = 0, QS_HEUR = 1, QS_LABEL = 2, QS_RASTER = 3, QS_COUNT = 4 };
-enum QueueCounter { QC_GRAPH = 0, QC_HEUR, QC_LOCAL, QC_MERGE, QC_FLATTEN, QC_RASTER, QC_COUNT };
+// the raster has one counter per tile shape (QC_RASTER + shape index)
+enum QueueCounter { QC_GRAPH = 0, QC_HEUR, QC_MERGE, QC_FLATTEN, QC_RASTER, QC_COUNT = QC_RASTER + 3 };
 
 struct QueueFrame {
     uint64_t in_off;  // bytes into the batch input (RGBA8, rows 4*w bytes)
@@ -78,7 +79,7 @@ struct QueueHeader {
     int32_t* labels;
     const QueueFrame* frames;
     const uint32_t* base;     // base[prefix * (n + 1) + f]: first tile of frame f
-    uint32_t total[6];        // tiles per prefix (kQPrefixes)
+    uint32_t total[9];        // tiles per prefix (kQPrefixes)
 };
 
 // Kernel parameters: fixed for a context, a scale and a launch shape, so a
@@ -91,16 +92,20 @@ struct QueueBatch {
     const uint32_t* lut;  // scale table
     int scale;
     int gran[QS_COUNT];   // tiles pulled per counter step, per stage
-    int rtw, rth;         // raster tile (cells)
+    int rtw, rth;         // raster tile (cells); 0, 0: each frame in its own shape
+    int rbase;            // first raster prefix: QS_RASTER (one shape for all) or kQMixedBase
 };
 
 // tiles of a frame per stage; the raster has three tile shapes, each with its
 // own prefix (QS_RASTER + shape index), so a batch can be raster-timed in
-// every shape without new descriptors
+// every shape without new descriptors, and three more prefixes in which each
+// frame counts only in the shape assigned to it (kQMixedBase + shape index:
+// the shape with the fewest cells to process, ring included)
 constexpr int kQGraphTW = 64, kQGraphTH = 16, kQHeurTW = 64, kQHeurTH = 16, kQLabelT = 32;
 constexpr int kQRasterShapes = 3;
-constexpr int kQPrefixes = QS_RASTER + kQRasterShapes;
-static_assert(kQPrefixes == 6, "QueueHeader::total");
+constexpr int kQMixedBase = QS_RASTER + kQRasterShapes;
+constexpr int kQPrefixes = kQMixedBase + kQRasterShapes;
+static_assert(kQPrefixes == 9, "QueueHeader::total");
 constexpr int kQRasterTW[kQRasterShapes] = {32, 32, 16}, kQRasterTH[kQRasterShapes] = {32, 16, 16};
 __host__ __device__ constexpr int raster_shape_index(int tw, int th)
 {
@@ -123,7 +128,8 @@ struct QueueCall {
     uint8_t* graph_a;
     uint8_t* graph_b;
 };
-// Launch shape of the queue path: granularity per stage and raster tile.
+// Launch shape of the queue path: granularity per stage and raster tile
+// (0 x 0: each frame in the tile shape assigned to it).
 struct QueueShape {
     int gran[QS_COUNT];
     int rtw, rth;

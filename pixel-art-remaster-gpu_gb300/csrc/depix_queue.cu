@@ -45,7 +45,8 @@ int log2_floor(uint64_t x)
 // Graph cache key: everything a captured graph bakes in besides the context.
 uint64_t graph_key(int scale, bool labels, const QueueShape& sh)
 {
-    uint64_t k = (uint64_t)scale | (uint64_t)labels << 8 | (uint64_t)raster_shape_index(sh.rtw, sh.rth) << 9;
+    const int shape = sh.rtw == 0 ? 3 : raster_shape_index(sh.rtw, sh.rth);
+    uint64_t k = (uint64_t)scale | (uint64_t)labels << 8 | (uint64_t)shape << 9;
     for (int st = 0; st < QS_COUNT; st++) k |= (uint64_t)log2_floor((uint64_t)sh.gran[st]) << (12 + 4 * st);
     return k;
 }
@@ -116,8 +117,31 @@ public:
         return v;
     }
 
+    // one raster launch per tile shape when each frame has its own shape
+    cudaError_t launch_mixed_raster(const QueueBatch& b, cudaStream_t s, bool trim)
+    {
+        for (int k = 0; k < kQRasterShapes; k++) {
+            QueueBatch bb = b;
+            bb.rtw = kQRasterTW[k];
+            bb.rth = kQRasterTH[k];
+            bb.rbase = kQMixedBase;
+            const int bps = blocks_per_sm(QS_RASTER, bb);
+            if (bps <= 0) return cudaErrorInvalidConfiguration;
+            int blocks = sms * bps;
+            if (trim) {
+                const uint32_t t = total[kQMixedBase + k];
+                if (t == 0) continue;
+                blocks = (int)std::min<uint32_t>((uint32_t)blocks, (t + bb.gran[QS_RASTER] - 1) / bb.gran[QS_RASTER]);
+            }
+            const cudaError_t e = queue_raster(bb, blocks, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+
     cudaError_t launch(int stage, const QueueBatch& b, cudaStream_t s, bool trim)
     {
+        if (stage == QS_RASTER && b.rtw == 0) return launch_mixed_raster(b, s, trim);
         const int bps = blocks_per_sm(stage, b);
         if (bps <= 0) return cudaErrorInvalidConfiguration;
         int blocks = sms * bps;
@@ -140,6 +164,7 @@ public:
         for (int st = 0; st < QS_COUNT; st++) b.gran[st] = sh.gran[st];
         b.rtw = sh.rtw;
         b.rth = sh.rth;
+        b.rbase = sh.rtw == 0 ? kQMixedBase : QS_RASTER;
         return b;
     }
 
@@ -233,14 +258,16 @@ depix_status QueueRunner::tune(cudaStream_t s, QueueShape* out)
             }
         }
     }
-    // the raster alone in the other tile shapes (the graph it reads is done)
-    for (int k = first_shape + 1; k < kQRasterShapes; k++) {
+    // the raster alone in the other tile shapes (the graph it reads is done),
+    // then with each frame in its own shape (k == kQRasterShapes)
+    for (int k = first_shape + 1; k <= kQRasterShapes; k++) {
         for (int g : grans) {
-            QueueShape sh{{g, g, g, g}, kQRasterTW[k], kQRasterTH[k]};
+            QueueShape sh{{g, g, g, g}, k < kQRasterShapes ? kQRasterTW[k] : 0,
+                          k < kQRasterShapes ? kQRasterTH[k] : 0};
             const QueueBatch b = batch_for(sh);
-            if (blocks_per_sm(QS_RASTER, b) <= 0) break;
+            if (sh.rtw != 0 && blocks_per_sm(QS_RASTER, b) <= 0) break;
             for (int rep = 0; rep < 3; rep++) {
-                cudaError_t e = cudaMemsetAsync(d_counters + QC_RASTER, 0, sizeof(int), s);
+                cudaError_t e = cudaMemsetAsync(d_counters + QC_RASTER, 0, kQRasterShapes * sizeof(int), s);
                 if (e == cudaSuccess) e = cudaEventRecord(tev[0], s);
                 if (e == cudaSuccess) e = launch(QS_RASTER, b, s, true);
                 if (e == cudaSuccess) e = cudaEventRecord(tev[1], s);
@@ -274,11 +301,24 @@ depix_status QueueRunner::graph_for(cudaGraphExec_t* out)
     }
     const QueueBatch b = batch_for(shape);
     // occupancy queries (and the raster's shared-memory opt-in) before capture
-    for (int st = 0; st < QS_COUNT; st++)
-        if ((st != QS_LABEL || labels) && blocks_per_sm(st, b) <= 0) {
+    for (int st = 0; st < QS_COUNT; st++) {
+        if (st == QS_LABEL && !labels) continue;
+        bool ok = true;
+        if (st == QS_RASTER && b.rtw == 0) {
+            for (int k = 0; k < kQRasterShapes; k++) {
+                QueueBatch bb = b;
+                bb.rtw = kQRasterTW[k];
+                bb.rth = kQRasterTH[k];
+                ok &= blocks_per_sm(QS_RASTER, bb) > 0;
+            }
+        } else {
+            ok = blocks_per_sm(st, b) > 0;
+        }
+        if (!ok) {
             set_last_error("a stage kernel cannot launch in this shape");
             return DEPIX_ERR_CUDA;
         }
+    }
     cudaError_t e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return fail(e, "cudaStreamBeginCapture");
     e = cudaMemsetAsync(d_counters, 0, QC_COUNT * sizeof(int), capture_stream);
@@ -318,10 +358,21 @@ depix_status queue_prepare(QueueRunner* r, const QueueCall& c, cudaStream_t s)
     for (int f = 0; f < n; f++) {
         const int w = c.w[f], hh = c.h[f];
         F[f] = QueueFrame{c.in_off[f], c.out_off[f], px, w, hh};
-        const uint32_t t[kQPrefixes] = {tiles(w, hh, kQGraphTW, kQGraphTH), tiles(w, hh, kQHeurTW, kQHeurTH),
-                                        tiles(w, hh, kQLabelT, kQLabelT),   tiles(w, hh, kQRasterTW[0], kQRasterTH[0]),
-                                        tiles(w, hh, kQRasterTW[1], kQRasterTH[1]),
-                                        tiles(w, hh, kQRasterTW[2], kQRasterTH[2])};
+        uint32_t t[kQPrefixes] = {tiles(w, hh, kQGraphTW, kQGraphTH), tiles(w, hh, kQHeurTW, kQHeurTH),
+                                  tiles(w, hh, kQLabelT, kQLabelT),   tiles(w, hh, kQRasterTW[0], kQRasterTH[0]),
+                                  tiles(w, hh, kQRasterTW[1], kQRasterTH[1]),
+                                  tiles(w, hh, kQRasterTW[2], kQRasterTH[2]), 0, 0, 0};
+        // the frame's own shape: fewest cells processed, each tile's ring included
+        int best = 0;
+        uint64_t best_cost = ~0ull;
+        for (int k = 0; k < kQRasterShapes; k++) {
+            const uint64_t cost = (uint64_t)t[QS_RASTER + k] * (kQRasterTW[k] + 2) * (kQRasterTH[k] + 2);
+            if (cost < best_cost) {
+                best_cost = cost;
+                best = k;
+            }
+        }
+        t[kQMixedBase + best] = t[QS_RASTER + best];
         for (int p = 0; p < kQPrefixes; p++) {
             base[p * (n + 1) + f] = (uint32_t)tot[p];
             tot[p] += t[p];
@@ -353,7 +404,7 @@ depix_status queue_prepare(QueueRunner* r, const QueueCall& c, cudaStream_t s)
 
     r->labels = c.labels != nullptr;
     r->q = QueueBatch{reinterpret_cast<const QueueHeader*>(r->d_desc), r->d_counters, c.graph_a, c.graph_b, c.lut,
-                      c.scale, {1, 1, 1, 1}, 32, 32};
+                      c.scale, {1, 1, 1, 1}, 32, 32, QS_RASTER};
     if (r->forced) {
         r->shape = r->force;
         return DEPIX_OK;

@@ -97,12 +97,12 @@ def test_uneven_batch_tuned_matches_oracle(cuda, scale):
     ctx = depix.Context(max(i.shape[0] * i.shape[1] for i in imgs), len(imgs))
     rasters, labs = _run(torch, ctx, imgs, scale)
     gran, tw, th = ctx.launch_shape()
-    assert all(g in (1, 2, 4, 8) for g in gran) and (tw, th) in ((32, 32), (32, 16), (16, 16))
+    assert all(g in (1, 2, 4, 8) for g in gran) and (tw, th) in ((32, 32), (32, 16), (16, 16), (0, 0))
     _check(imgs, scale, rasters, labs)
     ctx.close()
 
 
-@pytest.mark.parametrize("tile", [(32, 32), (32, 16), (16, 16)])
+@pytest.mark.parametrize("tile", [(32, 32), (32, 16), (16, 16), (0, 0)])
 @pytest.mark.parametrize("gran", [1, 8])
 def test_every_forced_shape_gives_the_same_bytes(cuda, tile, gran):
     import depix
