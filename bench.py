@@ -510,33 +510,49 @@ def run_stream(args, dev, stream):
     plain_lat = sorted(a.elapsed_time(b) for a, b in marks)
     ctx1.close()
 
-    # batched + refined with warm start
+    # batched + refined with warm start: a batch's eight topology setups run
+    # at once (each refiner on its own stream, driven from its own host
+    # thread: a setup reads its counts back), then warm start and Adam steps
+    # frame after frame (each frame starts from the previous frame's nodes)
+    from concurrent.futures import ThreadPoolExecutor
     ctx = depix.Context(W * H, B)
     d_in = torch.empty(B * fb, dtype=torch.uint8, device=dev)
     d_out = torch.empty(B * out_px * 4, dtype=torch.uint8, device=dev)
-    rfs = [depix.Refiner(W * H), depix.Refiner(W * H)]
+    rfs = [[depix.Refiner(W * H) for _ in range(B)] for _ in range(2)]  # one set per batch parity
     cap = 4 * W * H  # nodes never exceed a few per pixel
-    pos = [torch.empty(2 * cap, dtype=torch.float32, device=dev) for _ in range(2)]
+    pos = [[torch.empty(2 * cap, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(2)]
+    side = [torch.cuda.Stream(dev) for _ in range(B)]
+    pool = ThreadPoolExecutor(max_workers=B)
     in_off = [k * fb for k in range(B)]
     out_off = [k * out_px * 4 for k in range(B)]
+
+    def setup(rf, k, uploaded):
+        side[k].wait_event(uploaded)
+        rf.setup(d_in[k * fb:], W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp, stream=side[k])
+        assert rf.counts()["nodes"] <= cap
+        done = torch.cuda.Event()
+        done.record(side[k])
+        return done
 
     def run_all(count_reuse):
         reused, tiles = 0, 0
         prev = None
-        for b0 in range(0, n, B):
+        for bi, b0 in enumerate(range(0, n, B)):
             start = ev()
             start.record(stream)
             d_in.copy_(h_frames[b0:b0 + B].reshape(-1), non_blocking=True)
+            uploaded = torch.cuda.Event()
+            uploaded.record(stream)
             ctx.batch([W] * B, [H] * B, in_off, out_off, d_in, p, d_out, None, stream=stream)
+            cur = rfs[bi % 2]
+            futs = [pool.submit(setup, cur[k], k, uploaded) for k in range(B)]
             for k in range(B):
-                f = b0 + k
-                rf, ps = rfs[f % 2], pos[f % 2]
-                rf.setup(d_in[k * fb:], W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp, stream=stream)
-                assert rf.counts()["nodes"] <= cap
+                rf, ps = cur[k], pos[bi % 2][k]
+                stream.wait_event(futs[k].result())
                 if prev is None:
                     rf.initial(ps, stream=stream)
                 else:
-                    r = rf.warm_start(rfs[prev % 2], pos[prev % 2], ps, stream=stream, count=count_reuse)
+                    r = rf.warm_start(prev[0], prev[1], ps, stream=stream, count=count_reuse)
                     if count_reuse:
                         reused += r
                         tiles += ((W + 15) // 16) * ((H + 15) // 16)
@@ -544,7 +560,9 @@ def run_stream(args, dev, stream):
                 done = ev()
                 done.record(stream)
                 lat_marks.append((start, done))
-                prev = f
+                prev = (rf, ps)
+            # the next batch's upload is ordered after these steps on the main
+            # stream, and its setups (the other refiner set) wait for that upload
         return reused, tiles
 
     lat_marks = []
@@ -559,6 +577,10 @@ def run_stream(args, dev, stream):
     lat_marks = []
     reused, tiles = run_all(True)
     torch.cuda.synchronize()
+    pool.shutdown()
+    rfs_flat = [r for st in rfs for r in st]
+    rfs = [rfs_flat[0], rfs_flat[1]]
+    pos = [pos[0][0], pos[0][1]]
 
     # warm against cold start: energy after 20 steps on a few frames
     warm_e, cold_e = [], []
@@ -575,7 +597,7 @@ def run_stream(args, dev, stream):
         rf.warm_start(prv, pp, ps, stream=stream, count=False)
         warm_e.append(rf.run(rp, ps, stream=stream)[1][3])
         cold_e.append(rf.run(rp, None, stream=stream)[1][3])
-    for r in rfs:
+    for r in rfs_flat:
         r.close()
     ctx.close()
     pct = lambda v, q: round(v[min(len(v) - 1, int(q * len(v)))], 4)
