@@ -239,7 +239,7 @@ def run_ours(args, rank, world, local_rank):
     achieved = alg_bytes / (raster_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     tpf = profiled_traffic()
-    roofline = {"kernel": "k_mask_raster (cell masks, block resolution, 16-byte output stores)", "bound": "hbm",
+    roofline = {"kernel": "k_mask_raster_tma (TMA pixel windows, cell masks, block resolution, 16-byte output stores)", "bound": "hbm",
                 "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (tpf * B if tpf else None),
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": round(raster_ms, 4),

@@ -72,6 +72,10 @@ const char* depix_last_error(void);
  * the current device). Every entry point does it on first use on a device;
  * call it once before capturing any stream into a CUDA graph. */
 depix_status depix_init_device(void);
+/* Sticky device-side faults of the current device since the last call,
+ * then cleared: bit 0, a bounded wait for a TMA tile load gave up (that tile
+ * of the raster was left unwritten). Synchronous. */
+depix_status depix_take_device_faults(int* flags);
 
 /* ---------------------------------------------------------------------
  * Stage entry points: each mirrors one reference kernel, on device memory.

@@ -210,6 +210,16 @@ const char* depix_last_error(void) { return t_last_error.c_str(); }
 
 depix_status depix_init_device(void) { return ensure_tables(nullptr); }
 
+depix_status depix_take_device_faults(int* flags)
+{
+    if (!flags) return arg_fail("NULL flags");
+    *flags = 0;
+    int raster = 0;
+    DEPIX_CK(take_raster_fault(&raster));
+    *flags = raster ? 1 : 0;
+    return DEPIX_OK;
+}
+
 depix_status depix_graph(const uint8_t* d_img, int w, int h, int widthstep, depix_layout layout,
                          const depix_params* p, int fuse_trivial, uint8_t* d_graph, depix_stream s)
 {

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h> // CUtensorMap (the type only; the encoder comes through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/depix.h"
@@ -740,6 +741,50 @@ __device__ __forceinline__ bool star_crossing_mask(const Packed& P, int u, int m
     const uint32_t fmask = F >= 32 ? 0xFFFFFFFFu : ((1u << F) - 1u);
     for (int row = 0; row < F; row++) rows[row * rstride] &= fmask;
     return ok && wraps == 1;
+}
+
+// ------------------------------------------------- TMA tile loads (sm_90+)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Waits for the phase with the given parity to complete, at most max_iter
+// polls; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int max_iter)
+{
+    for (int i = 0; i < max_iter; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// One 3-D tile of a tensor map into shared memory, completing on bar. The
+// innermost coordinate times the element size must be a multiple of 16
+// bytes (the caller guarantees it); out-of-range elements read as zero.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
 }
 
 }  // namespace depix

@@ -619,6 +619,10 @@ cudaError_t build_scale_masks(int s, uint32_t* lut, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// set when a bounded wait for a TMA tile load gave up (the block then left
+// its tile unwritten); read and cleared by depix_take_device_faults
+__device__ int g_raster_fault;
+
 // slots of a tile's table of distinct cut polygons (bounded probing: a
 // polygon that finds no slot makes its own mask)
 constexpr int kPolyTable = 1024, kPolyProbes = 16;
@@ -628,8 +632,13 @@ struct MaskTile {
     static constexpr int GW = TW + 2, GH = TH + 2, GN = GW * GH; // cells with their ring
     static constexpr int BW = TW + 6, BH = TH + 6;               // graph, halo 3
     static constexpr int CW = TW + 4, CH = TH + 4;               // pixels, halo 2
+    // pixels with halo 2, stored from two columns further left (x0 - 4) so
+    // that a TMA box can start on a 16-byte boundary: pixel (lx, ly) of the
+    // halo-2 window is pix[ly][lx + 2]
+    __align__(128) uint32_t pix[CH][CW + 4];
+    uint64_t bar;      // completion of the TMA pixel load
+    int tma_ok;
     uint8_t graph[BH][BW];
-    uint32_t pix[CH][CW];
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
     uint8_t live[GN];  // the cell exists (inside the image)
     uint16_t list[GN]; // subdivided cells of the tile, then the blocks that need owner resolution
@@ -806,16 +815,25 @@ __device__ __forceinline__ uint64_t polygon_hash(const Packed& sp)
     return h;
 }
 
-template <int LAYOUT, int S, int TW, int TH>
+template <int LAYOUT, int S, int TW, int TH, bool TMA = false>
 __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
                                  uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
-                                 int y0)
+                                 int y0, const CUtensorMap* pix_map = nullptr, int frame = 0)
 {
     using T = MaskTile<TW, TH>;
     const int s = S > 0 ? S : scale;
     const MaskGeom G = mask_geom(s);
     const int F = G.F;
     // ---- phase A
+    if constexpr (TMA) {
+        // the pixel window (x0 - 4 .. x0 + TW + 4) x (y0 - 2 .. y0 + TH + 2) by
+        // one TMA tile load while the threads fetch the graph
+        if (threadIdx.x == 0) {
+            mbar_init(&M.bar, 1);
+            mbar_expect_tx(&M.bar, (uint32_t)sizeof(M.pix));
+            tma_load_3d(&M.pix[0][0], pix_map, x0 - 4, y0 - 2, frame, &M.bar);
+        }
+    }
     if (threadIdx.x == 0) {
         M.count = 0;
         M.slow = 0;
@@ -828,11 +846,26 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = __ldg(g + (size_t)gy * w + gx) & inside_mask(gx, gy, w, h);
         M.graph[k / T::BW][k % T::BW] = (uint8_t)v;
     }
-    for (int k = threadIdx.x; k < T::CW * T::CH; k += blockDim.x) {
-        int gx = x0 - 2 + k % T::CW, gy = y0 - 2 + k / T::CW;
-        uint32_t v = 0;
-        if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = load_bgr(img, ws, LAYOUT, gx, gy);
-        M.pix[k / T::CW][k % T::CW] = v;
+    if constexpr (TMA) {
+        // the box holds RGBA words; the tile works on the reference's byte
+        // order (b0, b1, b2) = (B, G, R), as load_bgr gives it
+        if (threadIdx.x == 0) {
+            M.tma_ok = mbar_wait_bounded(&M.bar, 0, 1 << 22) ? 1 : 0;
+            if (!M.tma_ok) atomicExch(&g_raster_fault, 1);
+        }
+        __syncthreads();
+        if (!M.tma_ok) return;
+        for (int k = threadIdx.x; k < T::CH * (T::CW + 4); k += blockDim.x) {
+            uint32_t& v = M.pix[k / (T::CW + 4)][k % (T::CW + 4)];
+            v = ((v >> 16) & 0xFFu) | (v & 0xFF00u) | ((v & 0xFFu) << 16);
+        }
+    } else {
+        for (int k = threadIdx.x; k < T::CW * T::CH; k += blockDim.x) {
+            int gx = x0 - 2 + k % T::CW, gy = y0 - 2 + k / T::CW;
+            uint32_t v = 0;
+            if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = load_bgr(img, ws, LAYOUT, gx, gy);
+            M.pix[k / T::CW][k % T::CW + 2] = v;
+        }
     }
     __syncthreads();
 
@@ -880,7 +913,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
             if (ci == 0 || ci == w - 1 || cj >= h - 1) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
             const int qx = lx + 1, qy = ly + 1;
-            auto C = [&](int dx, int dy) { return M.pix[qy + dy][qx + dx]; };
+            auto C = [&](int dx, int dy) { return M.pix[qy + dy][qx + dx + 2]; };
             if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
             if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
             if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
@@ -970,7 +1003,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             M.list[atomicAdd(&M.slow, 1)] = (uint16_t)q;
             continue;
         }
-        const uint32_t own_col = rgba_of(M.pix[ty + 2][tx + 2]);
+        const uint32_t own_col = rgba_of(M.pix[ty + 2][tx + 4]);
         uint8_t* orow = out + ((size_t)cj * s * ow + (size_t)ci * s) * 4;
         for (int r = 0; r < s; r++) {
             uint32_t* o = reinterpret_cast<uint32_t*>(orow + (size_t)r * ow * 4);
@@ -993,7 +1026,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         // the nine candidates' colours, in priority order
         uint32_t cand_col[9];
 #pragma unroll
-        for (int z = 0; z < 9; z++) cand_col[z] = rgba_of(M.pix[ty + 2 + 1 - z / 3][tx + 2 + 1 - z % 3]);
+        for (int z = 0; z < 9; z++) cand_col[z] = rgba_of(M.pix[ty + 2 + 1 - z / 3][tx + 4 + 1 - z % 3]);
         for (int r = 0; r < s; r++) {
             // per candidate (priority order q = 0..8: rows above first, then
             // right to left) the samples of this row it covers and no
@@ -1051,9 +1084,78 @@ __global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32
                                         blockIdx.x * 32, blockIdx.y * TH);
 }
 
+// The equal-size batch raster with its pixel windows loaded by TMA (RGBA
+// frames whose base, rows and frame stride are 16-byte aligned).
+template <int S, int TH>
+__global__ void __launch_bounds__(256, 3) k_mask_raster_tma(RasterBatch b, const uint32_t* lut,
+                                                         const __grid_constant__ CUtensorMap pix_map)
+{
+    __shared__ MaskTile<32, TH> M;
+    extern __shared__ uint32_t masks[];
+    size_t z = blockIdx.z;
+    mask_raster_tile<DEPIX_LAYOUT_RGBA, S, 32, TH, true>(M, masks, b.img + b.img_stride * z, b.ws,
+                                                         b.graph + b.graph_stride * z, b.out + b.out_stride * z, b.w,
+                                                         b.h, b.scale, b.subdivide != 0, lut, blockIdx.x * 32,
+                                                         blockIdx.y * TH, &pix_map, (int)z);
+}
+
+using TensorMapEncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                          const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                          CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                          CUtensorMapFloatOOBfill);
+
+static TensorMapEncodeTiled tensor_map_encoder()
+{
+    static TensorMapEncodeTiled fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<TensorMapEncodeTiled>(p);
+    }();
+    return fn;
+}
+
+// The pixel tensor map of a batch: RGBA words, (w, h, frames), a box of
+// (32 + 8) x (TH + 4) x 1. False when the batch does not meet TMA's rules
+// (16-byte aligned base, row and frame strides) or no encoder is available.
+static bool pixel_tensor_map(const RasterBatch& b, int nframes, int TH, CUtensorMap* map)
+{
+    if (b.layout != DEPIX_LAYOUT_RGBA) return false;
+    if ((reinterpret_cast<uintptr_t>(b.img) & 15) || (b.ws & 15)) return false;
+    const uint64_t fstride = nframes > 1 ? (uint64_t)b.img_stride : ((uint64_t)b.ws * b.h + 15) & ~15ull;
+    if (fstride & 15) return false;
+    const TensorMapEncodeTiled enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)b.w, (cuuint64_t)b.h, (cuuint64_t)nframes};
+    const cuuint64_t strides[2] = {(cuuint64_t)b.ws, (cuuint64_t)fstride};
+    const cuuint32_t box[3] = {32 + 8, (cuuint32_t)(TH + 4), 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint8_t*>(b.img), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int LAYOUT, int S, int TH>
 static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
 {
+    if constexpr (LAYOUT == DEPIX_LAYOUT_RGBA) {
+        CUtensorMap map;
+        if (pixel_tensor_map(b, nframes, TH, &map)) {
+            MaskGeom g = mask_geom(b.scale);
+            size_t smem = (size_t)MaskTile<32, TH>::GN * g.F * sizeof(uint32_t);
+            if (smem + sizeof(MaskTile<32, TH>) > 48 * 1024) {
+                cudaError_t e = cudaFuncSetAttribute(k_mask_raster_tma<S, TH>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return e;
+            }
+            dim3 grid((b.w + 32 - 1) / 32, (b.h + TH - 1) / TH, nframes);
+            k_mask_raster_tma<S, TH><<<grid, 256, smem, s>>>(b, lut, map);
+            return cudaGetLastError();
+        }
+    }
     MaskGeom g = mask_geom(b.scale);
     size_t smem = (size_t)MaskTile<32, TH>::GN * g.F * sizeof(uint32_t);
     if (smem + sizeof(MaskTile<32, TH>) > 48 * 1024) {
@@ -1160,6 +1262,14 @@ cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t
     if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 8, 16>(b, nframes, lut, s);
     if (b.scale < 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 32>(b, nframes, lut, s);
     return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 16>(b, nframes, lut, s);
+}
+
+cudaError_t take_raster_fault(int* out)
+{
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_raster_fault, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_raster_fault, &zero, sizeof(int));
+    return e;
 }
 
 size_t scale_mask_words(int s) { return (size_t)4096 * mask_geom(s).HF; }

@@ -187,6 +187,8 @@ cudaError_t launch_raster(const RasterBatch& b, int nframes, cudaStream_t s);
 // coverage-mask raster (scale <= kMaxMaskScale) and its per-scale pattern table
 constexpr int kMaxMaskScale = 12;
 size_t scale_mask_words(int scale);
+// reads and clears the raster's sticky fault flag (a TMA wait that gave up)
+cudaError_t take_raster_fault(int* out);
 cudaError_t build_scale_masks(int scale, uint32_t* lut, cudaStream_t s);
 cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s);
 

@@ -65,6 +65,7 @@ def lib():
         _sig(L, "depix_status_string", [_i], ctypes.c_char_p)
         _sig(L, "depix_last_error", [], ctypes.c_char_p)
         _sig(L, "depix_init_device", [])
+        _sig(L, "depix_take_device_faults", [_vp])
         _sig(L, "depix_graph", [_vp, _i, _i, _i, _i, P, _i, _vp, _vp])
         _sig(L, "depix_resolve_trivial", [_vp, _i, _i, _vp])
         _sig(L, "depix_resolve_heuristics", [_vp, _i, _i, _vp, _vp])
@@ -262,6 +263,13 @@ class Context:
         ca = (ctypes.c_longlong * 4)()
         _check(lib().depix_context_stage_times(self.handle, ms, la, ca), "depix_context_stage_times")
         return {name: (ms[k], la[k], ca[k]) for k, name in enumerate(self.STAGES)}
+
+
+def take_device_faults() -> int:
+    """Sticky device-side fault bits since the last call (0: none)."""
+    f = ctypes.c_int(0)
+    _check(lib().depix_take_device_faults(ctypes.byref(f)), "depix_take_device_faults")
+    return f.value
 
 
 class Refiner:
