@@ -73,8 +73,9 @@ const char* depix_last_error(void);
  * call it once before capturing any stream into a CUDA graph. */
 depix_status depix_init_device(void);
 /* Sticky device-side faults of the current device since the last call,
- * then cleared: bit 0, a bounded wait for a TMA tile load gave up (that tile
- * of the raster was left unwritten). Synchronous. */
+ * then cleared: a bounded wait for a TMA tile load gave up and that tile
+ * was left unwritten, bit 0 in the raster, bit 1 in the graph stage.
+ * Synchronous. */
 depix_status depix_take_device_faults(int* flags);
 
 /* ---------------------------------------------------------------------

@@ -214,9 +214,10 @@ depix_status depix_take_device_faults(int* flags)
 {
     if (!flags) return arg_fail("NULL flags");
     *flags = 0;
-    int raster = 0;
+    int raster = 0, graph = 0;
     DEPIX_CK(take_raster_fault(&raster));
-    *flags = raster ? 1 : 0;
+    DEPIX_CK(take_graph_fault(&graph));
+    *flags = (raster ? 1 : 0) | (graph ? 2 : 0);
     return DEPIX_OK;
 }
 

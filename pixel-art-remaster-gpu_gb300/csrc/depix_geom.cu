@@ -1099,10 +1099,35 @@ __global__ void __launch_bounds__(256, 3) k_mask_raster_tma(RasterBatch b, const
                                                          blockIdx.y * TH, &pix_map, (int)z);
 }
 
+bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stride, int nframes, int box_w, int box_h,
+                     CUtensorMap* map);
+
 using TensorMapEncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                           const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
                                           CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
                                           CUtensorMapFloatOOBfill);
+
+static TensorMapEncodeTiled tensor_map_encoder();
+
+// A tensor map of RGBA frames as words, (w, h, frames), box (box_w, box_h, 1).
+// False when the frames do not meet TMA's rules (16-byte aligned base, row
+// and frame strides) or no encoder is available.
+bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stride, int nframes, int box_w, int box_h,
+                     CUtensorMap* map)
+{
+    if ((reinterpret_cast<uintptr_t>(img) & 15) || (ws & 15) || w < 1 || h < 1) return false;
+    const uint64_t fstride = nframes > 1 ? (uint64_t)frame_stride : ((uint64_t)ws * h + 15) & ~15ull;
+    if (fstride & 15) return false;
+    const TensorMapEncodeTiled enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)nframes};
+    const cuuint64_t strides[2] = {(cuuint64_t)ws, (cuuint64_t)fstride};
+    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint8_t*>(img), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 static TensorMapEncodeTiled tensor_map_encoder()
 {
@@ -1118,24 +1143,10 @@ static TensorMapEncodeTiled tensor_map_encoder()
     return fn;
 }
 
-// The pixel tensor map of a batch: RGBA words, (w, h, frames), a box of
-// (32 + 8) x (TH + 4) x 1. False when the batch does not meet TMA's rules
-// (16-byte aligned base, row and frame strides) or no encoder is available.
 static bool pixel_tensor_map(const RasterBatch& b, int nframes, int TH, CUtensorMap* map)
 {
     if (b.layout != DEPIX_LAYOUT_RGBA) return false;
-    if ((reinterpret_cast<uintptr_t>(b.img) & 15) || (b.ws & 15)) return false;
-    const uint64_t fstride = nframes > 1 ? (uint64_t)b.img_stride : ((uint64_t)b.ws * b.h + 15) & ~15ull;
-    if (fstride & 15) return false;
-    const TensorMapEncodeTiled enc = tensor_map_encoder();
-    if (!enc) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)b.w, (cuuint64_t)b.h, (cuuint64_t)nframes};
-    const cuuint64_t strides[2] = {(cuuint64_t)b.ws, (cuuint64_t)fstride};
-    const cuuint32_t box[3] = {32 + 8, (cuuint32_t)(TH + 4), 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint8_t*>(b.img), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return rgba_tensor_map(b.img, b.w, b.h, b.ws, b.img_stride, nframes, 32 + 8, TH + 4, map);
 }
 
 template <int LAYOUT, int S, int TH>

@@ -12,22 +12,54 @@ namespace depix {
 // Pair bits of one pixel p inside the tile region: similarity with the
 // right (bit 0), upper (bit 1), upper-right (bit 2) pixel, and of the pair
 // (right, upper) (bit 3), each only when both pixels are in the image.
+// set when a bounded wait for a TMA tile load gave up (that tile of the
+// graph was left unwritten); read and cleared by depix_take_device_faults
+__device__ int g_graph_fault;
+
 constexpr int kGTW = 64;  // graph tile width (pixels)
 constexpr int kGTH = 16;  // graph tile height
 
-template <int LAYOUT>
-__device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uint32_t thr, bool fuse_trivial)
+// the pixel window of a graph tile as one TMA box: RGBA words from x0 - 4
+// (16-byte aligned), y0 - 1, (kGTW + 8) x (kGTH + 2)
+constexpr int kGBoxW = kGTW + 8, kGBoxH = kGTH + 2;
+
+template <int LAYOUT, bool TMA = false>
+__device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uint32_t thr, bool fuse_trivial,
+                                           const CUtensorMap* pix_map = nullptr, int frame = 0)
 {
     constexpr int RW = kGTW + 2, RH = kGTH + 2;
     __shared__ uint32_t words[RH][RW];
     __shared__ uint8_t pairs[RH][RW];
     const int w = f.w, h = f.h;
-    for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
-        int rx = k % RW, ry = k / RW;
-        int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
-        uint32_t wd = 0;
-        if (gx >= 0 && gy >= 0 && gx < w && gy < h) wd = word_of_bgr(load_bgr(f.img, f.ws, LAYOUT, gx, gy));
-        words[ry][rx] = wd;
+    if constexpr (TMA) {
+        __shared__ __align__(128) uint32_t box[kGBoxH][kGBoxW];
+        __shared__ uint64_t bar;
+        __shared__ int ok;
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            mbar_expect_tx(&bar, (uint32_t)sizeof(box));
+            tma_load_3d(&box[0][0], pix_map, x0 - 4, y0 - 1, frame, &bar);
+            ok = mbar_wait_bounded(&bar, 0, 1 << 22) ? 1 : 0;
+            if (!ok) atomicExch(&g_graph_fault, 1);
+        }
+        __syncthreads();
+        if (!ok) return;
+        for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
+            const int rx = k % RW, ry = k / RW;
+            const uint32_t p = box[ry][rx + 3]; // window column rx is image column x0 - 1 + rx
+            // RGBA -> the reference's byte order (b0, b1, b2) = (B, G, R); zero outside the image
+            const uint32_t c = ((p >> 16) & 0xFFu) | (p & 0xFF00u) | ((p & 0xFFu) << 16);
+            const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+            words[ry][rx] = (gx >= 0 && gy >= 0 && gx < w && gy < h) ? word_of_bgr(c) : 0u;
+        }
+    } else {
+        for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
+            int rx = k % RW, ry = k / RW;
+            int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+            uint32_t wd = 0;
+            if (gx >= 0 && gy >= 0 && gx < w && gy < h) wd = word_of_bgr(load_bgr(f.img, f.ws, LAYOUT, gx, gy));
+            words[ry][rx] = wd;
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
@@ -89,6 +121,16 @@ __global__ void __launch_bounds__(256) k_graph(FrameBatch b, uint32_t thr, int f
 {
     FrameRef f = b.frame(blockIdx.z);
     graph_tile<LAYOUT>(f, blockIdx.x * kGTW, blockIdx.y * kGTH, thr, fuse_trivial != 0);
+}
+
+// RGBA frames whose base, rows and frame stride are 16-byte aligned: the
+// pixel windows come by TMA
+__global__ void __launch_bounds__(256) k_graph_tma(FrameBatch b, uint32_t thr, int fuse_trivial,
+                                                   const __grid_constant__ CUtensorMap pix_map)
+{
+    FrameRef f = b.frame(blockIdx.z);
+    graph_tile<DEPIX_LAYOUT_RGBA, true>(f, blockIdx.x * kGTW, blockIdx.y * kGTH, thr, fuse_trivial != 0, &pix_map,
+                                        (int)blockIdx.z);
 }
 
 // Trivial removal on a graph in place (crossCheck_4, graph_functions.cu:1211-1274).
@@ -595,10 +637,22 @@ cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, uint32_t* out, cudaSt
     return cudaGetLastError();
 }
 
+cudaError_t take_graph_fault(int* out)
+{
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_graph_fault, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_graph_fault, &zero, sizeof(int));
+    return e;
+}
+
 cudaError_t launch_graph(const FrameBatch& b, int nframes, uint32_t thr, bool fuse_trivial, cudaStream_t s)
 {
     dim3 grid((b.w + kGTW - 1) / kGTW, (b.h + kGTH - 1) / kGTH, nframes);
-    if (b.layout == DEPIX_LAYOUT_RGBA)
+    CUtensorMap map;
+    if (b.layout == DEPIX_LAYOUT_RGBA &&
+        rgba_tensor_map(b.img, b.w, b.h, b.ws, b.img_stride, nframes, kGBoxW, kGBoxH, &map))
+        k_graph_tma<<<grid, 256, 0, s>>>(b, thr, fuse_trivial ? 1 : 0, map);
+    else if (b.layout == DEPIX_LAYOUT_RGBA)
         k_graph<DEPIX_LAYOUT_RGBA><<<grid, 256, 0, s>>>(b, thr, fuse_trivial ? 1 : 0);
     else
         k_graph<DEPIX_LAYOUT_BGR><<<grid, 256, 0, s>>>(b, thr, fuse_trivial ? 1 : 0);

@@ -187,8 +187,14 @@ cudaError_t launch_raster(const RasterBatch& b, int nframes, cudaStream_t s);
 // coverage-mask raster (scale <= kMaxMaskScale) and its per-scale pattern table
 constexpr int kMaxMaskScale = 12;
 size_t scale_mask_words(int scale);
-// reads and clears the raster's sticky fault flag (a TMA wait that gave up)
+// reads and clears the raster's and the graph stage's sticky fault flags (a
+// TMA wait that gave up)
 cudaError_t take_raster_fault(int* out);
+cudaError_t take_graph_fault(int* out);
+// tensor map of RGBA frames as words, (w, h, frames), box (box_w, box_h, 1);
+// false when the buffers do not meet TMA's alignment rules
+bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stride, int nframes, int box_w, int box_h,
+                     CUtensorMap* map);
 cudaError_t build_scale_masks(int scale, uint32_t* lut, cudaStream_t s);
 cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s);
 
