@@ -166,7 +166,7 @@ def measured_peak():
 
 def profiled_traffic():
     """DRAM bytes per frame of the raster kernel from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "k_mask_raster_256x224_x4.md")
+    path = os.path.join(REPO, "profiles", "k_mask_raster_tma_256x224_x4.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_frame:"):
