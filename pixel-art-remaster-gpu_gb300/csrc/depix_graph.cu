@@ -458,7 +458,7 @@ constexpr int kLBorder = 4 * kLT - 4;
 
 // unions of border pixel q (of 2 TW + 2 (TH - 2)) of tile `tile` in a TW x TH
 // tiling with neighbours in other tiles
-template <int TW, int TH>
+template <int TW, int TH, bool SYMMETRIC = false>
 __device__ __forceinline__ void cc_merge_border_t(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
 {
     const int tiles_x = (w + TW - 1) / TW;
@@ -478,6 +478,9 @@ __device__ __forceinline__ void cc_merge_border_t(const uint8_t* g, int32_t* L, 
         int ni = i + dir_di(e), nj = j + dir_dj(e);
         if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
         if (ni / TW == i / TW && nj / TH == j / TH) continue;
+        // a symmetric graph (the resolved graph of this pipeline) holds each
+        // pair from both ends: unite it once, from the lower index
+        if (SYMMETRIC && nj * w + ni < k) continue;
         uf_unite(L, k, nj * w + ni);
     }
 }
@@ -495,8 +498,8 @@ __global__ void k_cc_merge_h(const uint8_t* g, int32_t* L, int w, int h, size_t 
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
     if (t / kHBorder >= tiles) return;
-    cc_merge_border_t<kHTW, kHTH>(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, t / kHBorder,
-                                  t % kHBorder);
+    cc_merge_border_t<kHTW, kHTH, true>(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h,
+                                        t / kHBorder, t % kHBorder);
 }
 
 __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
@@ -512,7 +515,8 @@ __global__ void k_cc_flatten(int32_t* L, int n, size_t frame_stride)
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     L += frame_stride * blockIdx.z;
-    L[k] = uf_find(L, k);
+    const int r = uf_find(L, k);
+    if (L[k] != r) L[k] = r;
 }
 
 // ------------------------------------------------ uneven batches (queue)
@@ -556,8 +560,8 @@ __global__ void __launch_bounds__(128) k_label_merge_queue(QueueBatch q)
         const int f = queue_frame(base, n, (uint32_t)t);
         const QueueFrame fr = H->frames[f];
         for (int b = threadIdx.x; b < kHBorder; b += blockDim.x)
-            cc_merge_border_t<kHTW, kHTH>(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h,
-                                          t - (int)base[f], b);
+            cc_merge_border_t<kHTW, kHTH, true>(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h,
+                                                t - (int)base[f], b);
     });
 }
 
