@@ -74,7 +74,8 @@ const char* depix_last_error(void);
 depix_status depix_init_device(void);
 /* Sticky device-side faults of the current device since the last call,
  * then cleared: a bounded wait for a TMA tile load gave up and that tile
- * was left unwritten, bit 0 in the raster, bit 1 in the graph stage.
+ * was left unwritten, bit 0 in the raster, bit 1 in the graph stage, bit 2
+ * in the heuristics stage.
  * Synchronous. */
 depix_status depix_take_device_faults(int* flags);
 

@@ -214,10 +214,11 @@ depix_status depix_take_device_faults(int* flags)
 {
     if (!flags) return arg_fail("NULL flags");
     *flags = 0;
-    int raster = 0, graph = 0;
+    int raster = 0, graph = 0, heur = 0;
     DEPIX_CK(take_raster_fault(&raster));
     DEPIX_CK(take_graph_fault(&graph));
-    *flags = (raster ? 1 : 0) | (graph ? 2 : 0);
+    DEPIX_CK(take_heuristics_fault(&heur));
+    *flags = (raster ? 1 : 0) | (graph ? 2 : 0) | (heur ? 4 : 0);
     return DEPIX_OK;
 }
 

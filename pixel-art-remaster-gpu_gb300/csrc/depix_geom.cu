@@ -1129,6 +1129,25 @@ bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stri
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// A tensor map of 8-bit frames (graph bytes), (w, h, frames), box (box_w,
+// box_h, 1); false when the buffers do not meet TMA's rules.
+bool u8_tensor_map(const uint8_t* base, int w, int h, size_t frame_stride, int nframes, int box_w, int box_h,
+                   CUtensorMap* map)
+{
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || (w & 15) || w < 1 || h < 1) return false;
+    const uint64_t fstride = nframes > 1 ? (uint64_t)frame_stride : ((uint64_t)w * h + 15) & ~15ull;
+    if (fstride & 15) return false;
+    const TensorMapEncodeTiled enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)nframes};
+    const cuuint64_t strides[2] = {(cuuint64_t)w, (cuuint64_t)fstride};
+    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static TensorMapEncodeTiled tensor_map_encoder()
 {
     static TensorMapEncodeTiled fn = [] {

@@ -15,6 +15,7 @@ namespace depix {
 // set when a bounded wait for a TMA tile load gave up (that tile of the
 // graph was left unwritten); read and cleared by depix_take_device_faults
 __device__ int g_graph_fault;
+__device__ int g_heur_fault; // the same for the heuristics stage
 
 constexpr int kGTW = 64;  // graph tile width (pixels)
 constexpr int kGTH = 16;  // graph tile height
@@ -229,11 +230,28 @@ __device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t
 // component labels too (union-find over the resolved bytes, still in shared
 // memory), which leaves the label stage only the merge across tile borders
 // and the flattening.
+template <bool TMA = false>
 __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* out, int w, int h, int x0, int y0,
-                                                int32_t* L = nullptr)
+                                                int32_t* L = nullptr, const CUtensorMap* map = nullptr,
+                                                int frame = 0)
 {
-    __shared__ __align__(16) uint8_t s[kHRH][kHRW];
+    __shared__ __align__(128) uint8_t s[kHRH][kHRW];
     const int ox = x0 - kHalo, oy = y0 - kHalo;
+    if constexpr (TMA) {
+        // the window as one TMA box (x0 - 32 is a multiple of 16 bytes);
+        // bytes outside the image read as zero
+        __shared__ uint64_t bar;
+        __shared__ int ok;
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            mbar_expect_tx(&bar, (uint32_t)sizeof(s));
+            tma_load_3d(&s[0][0], map, ox, oy, frame, &bar);
+            ok = mbar_wait_bounded(&bar, 0, 1 << 22) ? 1 : 0;
+            if (!ok) atomicExch(&g_heur_fault, 1);
+        }
+        __syncthreads();
+        if (!ok) return;
+    } else
     // 4-byte loads where a row is word aligned in memory, else bytes
     for (int k = threadIdx.x; k < kHRH * (kHRW / 4); k += blockDim.x) {
         int ry = k / (kHRW / 4), rx = 4 * (k % (kHRW / 4));
@@ -306,6 +324,16 @@ __global__ void __launch_bounds__(256) k_heuristics_labels(GraphBatch b, int32_t
     const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
     uint8_t* out = b.out + b.frame_stride * blockIdx.z;
     heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH, L + b.frame_stride * blockIdx.z);
+}
+
+// the same with the graph windows by TMA (width and frame stride multiples of
+// 16 bytes, 16-byte aligned base); L may be NULL
+__global__ void __launch_bounds__(256) k_heuristics_tma(GraphBatch b, int32_t* L, const __grid_constant__ CUtensorMap map)
+{
+    const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
+    uint8_t* out = b.out + b.frame_stride * blockIdx.z;
+    heuristics_tile<true>(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH,
+                          L ? L + b.frame_stride * blockIdx.z : nullptr, &map, (int)blockIdx.z);
 }
 
 // -------------------------------------------------- component labelling
@@ -673,15 +701,31 @@ cudaError_t launch_trivial(uint8_t* g, int w, int h, cudaStream_t s)
 cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s)
 {
     dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
-    k_heuristics<<<grid, 256, 0, s>>>(b);
+    CUtensorMap map;
+    if (u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map))
+        k_heuristics_tma<<<grid, 256, 0, s>>>(b, nullptr, map);
+    else
+        k_heuristics<<<grid, 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_heuristics_labels(const GraphBatch& b, int nframes, int32_t* labels, cudaStream_t s)
 {
     dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
-    k_heuristics_labels<<<grid, 256, 0, s>>>(b, labels);
+    CUtensorMap map;
+    if (u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map))
+        k_heuristics_tma<<<grid, 256, 0, s>>>(b, labels, map);
+    else
+        k_heuristics_labels<<<grid, 256, 0, s>>>(b, labels);
     return cudaGetLastError();
+}
+
+cudaError_t take_heuristics_fault(int* out)
+{
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_heur_fault, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_heur_fault, &zero, sizeof(int));
+    return e;
 }
 
 cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, int w, int h, int nframes,

@@ -191,6 +191,9 @@ size_t scale_mask_words(int scale);
 // TMA wait that gave up)
 cudaError_t take_raster_fault(int* out);
 cudaError_t take_graph_fault(int* out);
+cudaError_t take_heuristics_fault(int* out);
+bool u8_tensor_map(const uint8_t* base, int w, int h, size_t frame_stride, int nframes, int box_w, int box_h,
+                   CUtensorMap* map);
 // tensor map of RGBA frames as words, (w, h, frames), box (box_w, box_h, 1);
 // false when the buffers do not meet TMA's alignment rules
 bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stride, int nframes, int box_w, int box_h,
