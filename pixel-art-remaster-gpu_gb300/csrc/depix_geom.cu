@@ -638,7 +638,11 @@ struct MaskTile {
     __align__(128) uint32_t pix[CH][CW + 4];
     uint64_t bar;      // completion of the TMA pixel load
     int tma_ok;
-    uint8_t graph[BH][BW];
+    // graph bytes with halo 3, stored from 13 columns further left (x0 - 16)
+    // so that a TMA box starts on a 16-byte boundary: graph byte (bx, by) of
+    // the halo-3 window is graph[by][bx + kGOff]
+    static constexpr int kGOff = 13, GRW = TW + 32;
+    __align__(128) uint8_t graph[BH][GRW];
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
     uint8_t live[GN];  // the cell exists (inside the image)
     uint16_t list[GN]; // subdivided cells of the tile, then the blocks that need owner resolution
@@ -818,7 +822,8 @@ __device__ __forceinline__ uint64_t polygon_hash(const Packed& sp)
 template <int LAYOUT, int S, int TW, int TH, bool TMA = false>
 __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uint8_t* img, int ws, const uint8_t* g,
                                  uint8_t* out, int w, int h, int scale, bool subdivide, const uint32_t* lut, int x0,
-                                 int y0, const CUtensorMap* pix_map = nullptr, int frame = 0)
+                                 int y0, const CUtensorMap* pix_map = nullptr, int frame = 0,
+                                 const CUtensorMap* graph_map = nullptr)
 {
     using T = MaskTile<TW, TH>;
     const int s = S > 0 ? S : scale;
@@ -826,12 +831,14 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
     const int F = G.F;
     // ---- phase A
     if constexpr (TMA) {
-        // the pixel window (x0 - 4 .. x0 + TW + 4) x (y0 - 2 .. y0 + TH + 2) by
-        // one TMA tile load while the threads fetch the graph
+        // the pixel window (x0 - 4 .. x0 + TW + 4) x (y0 - 2 .. y0 + TH + 2)
+        // and, with a graph map, the graph window (x0 - 16 .. x0 + TW + 16) x
+        // (y0 - 3 .. y0 + TH + 3) by TMA tile loads on one barrier
         if (threadIdx.x == 0) {
             mbar_init(&M.bar, 1);
-            mbar_expect_tx(&M.bar, (uint32_t)sizeof(M.pix));
+            mbar_expect_tx(&M.bar, (uint32_t)(sizeof(M.pix) + (graph_map ? sizeof(M.graph) : 0)));
             tma_load_3d(&M.pix[0][0], pix_map, x0 - 4, y0 - 2, frame, &M.bar);
+            if (graph_map) tma_load_3d(&M.graph[0][0], graph_map, x0 - T::kGOff - 3, y0 - 3, frame, &M.bar);
         }
     }
     if (threadIdx.x == 0) {
@@ -840,11 +847,13 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         M.nreps = 0;
     }
     for (int k = threadIdx.x; k < kPolyTable; k += blockDim.x) M.table[k] = 0ull;
-    for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
-        int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
-        unsigned v = 0;
-        if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = __ldg(g + (size_t)gy * w + gx) & inside_mask(gx, gy, w, h);
-        M.graph[k / T::BW][k % T::BW] = (uint8_t)v;
+    if (!(TMA && graph_map)) {
+        for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
+            int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
+            unsigned v = 0;
+            if (gx >= 0 && gy >= 0 && gx < w && gy < h) v = __ldg(g + (size_t)gy * w + gx) & inside_mask(gx, gy, w, h);
+            M.graph[k / T::BW][k % T::BW + T::kGOff] = (uint8_t)v;
+        }
     }
     if constexpr (TMA) {
         // the box holds RGBA words; the tile works on the reference's byte
@@ -858,6 +867,15 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         for (int k = threadIdx.x; k < T::CH * (T::CW + 4); k += blockDim.x) {
             uint32_t& v = M.pix[k / (T::CW + 4)][k % (T::CW + 4)];
             v = ((v >> 16) & 0xFFu) | (v & 0xFF00u) | ((v & 0xFFu) << 16);
+        }
+        // graph bytes on the image's edge lose their bits toward outside (the
+        // box reads zero beyond the image); only tiles that reach an edge
+        if (graph_map && (x0 < 3 || y0 < 3 || x0 + TW + 3 > w || y0 + TH + 3 > h)) {
+            for (int k = threadIdx.x; k < T::BW * T::BH; k += blockDim.x) {
+                const int gx = x0 - 3 + k % T::BW, gy = y0 - 3 + k / T::BW;
+                if (gx >= 0 && gy >= 0 && gx < w && gy < h)
+                    M.graph[k / T::BW][k % T::BW + T::kGOff] &= (uint8_t)inside_mask(gx, gy, w, h);
+            }
         }
     } else {
         for (int k = threadIdx.x; k < T::CW * T::CH; k += blockDim.x) {
@@ -882,13 +900,13 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             continue;
         }
         const int bx = lx + 2, by = ly + 2;
-        unsigned node = M.graph[by][bx];
+        unsigned node = M.graph[by][bx + T::kGOff];
         if (subdivide && node != 90) {
             int slot = atomicAdd(&M.count, 1);
             M.list[slot] = (uint16_t)k;
             continue;
         }
-        int pat = cell_pattern(node, M.graph[by][bx - 1], M.graph[by][bx + 1]);
+        int pat = cell_pattern(node, M.graph[by][bx - 1 + T::kGOff], M.graph[by][bx + 1 + T::kGOff]);
         const int dr = G.hlo - G.mlo; // hull window row/column offset inside the footprint
         const uint32_t* src = lut + (size_t)pat * G.HF;
         for (int r = 0; r < F; r++) {
@@ -906,7 +924,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         int lx = k % T::GW, ly = k / T::GW;
         int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
         const int bx = lx + 2, by = ly + 2;
-        auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx]; };
+        auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx + T::kGOff]; };
         auto tj = [&](int px, int py) -> bool {
             long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
             long long index = (long long)cj * st + (long long)ci * 3;
@@ -1088,7 +1106,8 @@ __global__ void __launch_bounds__(256) k_mask_raster(RasterBatch b, const uint32
 // frames whose base, rows and frame stride are 16-byte aligned).
 template <int S, int TH>
 __global__ void __launch_bounds__(256, 3) k_mask_raster_tma(RasterBatch b, const uint32_t* lut,
-                                                         const __grid_constant__ CUtensorMap pix_map)
+                                                         const __grid_constant__ CUtensorMap pix_map,
+                                                         const __grid_constant__ CUtensorMap graph_map, int with_graph)
 {
     __shared__ MaskTile<32, TH> M;
     extern __shared__ uint32_t masks[];
@@ -1096,7 +1115,8 @@ __global__ void __launch_bounds__(256, 3) k_mask_raster_tma(RasterBatch b, const
     mask_raster_tile<DEPIX_LAYOUT_RGBA, S, 32, TH, true>(M, masks, b.img + b.img_stride * z, b.ws,
                                                          b.graph + b.graph_stride * z, b.out + b.out_stride * z, b.w,
                                                          b.h, b.scale, b.subdivide != 0, lut, blockIdx.x * 32,
-                                                         blockIdx.y * TH, &pix_map, (int)z);
+                                                         blockIdx.y * TH, &pix_map, (int)z,
+                                                         with_graph ? &graph_map : nullptr);
 }
 
 bool rgba_tensor_map(const uint8_t* img, int w, int h, int ws, size_t frame_stride, int nframes, int box_w, int box_h,
@@ -1181,8 +1201,12 @@ static cudaError_t launch_mask_raster_t(const RasterBatch& b, int nframes, const
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                 if (e != cudaSuccess) return e;
             }
+            // the graph window too, when the graph's width and frame stride allow it
+            CUtensorMap gmap;
+            const bool with_graph = u8_tensor_map(b.graph, b.w, b.h, b.graph_stride, nframes, 32 + 32, TH + 6, &gmap);
+            if (!with_graph) gmap = map; // unused
             dim3 grid((b.w + 32 - 1) / 32, (b.h + TH - 1) / TH, nframes);
-            k_mask_raster_tma<S, TH><<<grid, 256, smem, s>>>(b, lut, map);
+            k_mask_raster_tma<S, TH><<<grid, 256, smem, s>>>(b, lut, map, gmap, with_graph ? 1 : 0);
             return cudaGetLastError();
         }
     }
