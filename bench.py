@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--no-sprites", action="store_true")
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-stream", action="store_true")
+    ap.add_argument("--no-vote", action="store_true")
     ap.add_argument("--stream-frames", type=int, default=512)
     return ap.parse_args()
 
@@ -288,6 +289,27 @@ def run_ours(args, rank, world, local_rank):
              "p99_ms_per_frame": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4), "frames": pf}
     ctx1.close()
 
+    # the same batch with the weighted-vote heuristics (depix_params.vote)
+    vote = None
+    if not args.no_vote:
+        pv = depix.params(48, 7, 6, True, SCALE, vote=True)
+        for _ in range(3):
+            ctx.batch(ws, hs, in_off, out_off, d_in, pv, d_out, d_lab, stream=stream)
+        torch.cuda.synchronize()
+        ctx.stage_times()
+        ctx.set_timing(True)
+        vsteps = max(10, args.steps // 10)
+        e0.record(stream)
+        for _ in range(vsteps):
+            ctx.batch(ws, hs, in_off, out_off, d_in, pv, d_out, d_lab, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.set_timing(False)
+        vst = ctx.stage_times()
+        vms = e0.elapsed_time(e1)
+        vote = {"frames_per_s": round(B * vsteps / (vms / 1e3), 1), "ms_per_step": round(vms / vsteps, 4),
+                "steps": vsteps, "stage_ms_per_step": {k: round(v[0] / max(v[2], 1), 4) for k, v in vst.items()}}
+
     sprites = None if args.no_sprites else run_sprites(args, dev, stream)
     refine = None if args.no_refine else run_refine(args, dev, stream, cpu=(rank == 0 and world == 1 and not args.no_cpu))
     stream_leg = None if args.no_stream else run_stream(args, dev, stream)
@@ -308,7 +330,7 @@ def run_ours(args, rank, world, local_rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
-                "refine": refine, "stream": stream_leg}
+                "refine": refine, "stream": stream_leg, "vote": vote}
         print(json.dumps(line))
 
 

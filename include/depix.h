@@ -61,6 +61,13 @@ typedef struct depix_params {
     int tr_y, tr_u, tr_v;
     int subdivide; /* run the corner-cutting stage (simpleVBO.cpp:41 default off) */
     int scale;     /* raster scale factor, 1..64 */
+    /* heuristic crossing resolution: 0 (default) the reference's ordered
+     * tests (processHeuristics2, graph_functions.cu:761-849); 1 the weighted
+     * vote of Kopf and Lischinski, "Depixelizing Pixel Art" (2011) sec. 3.2:
+     * curves, sparse pixels (component sizes in the 8x8 window around the
+     * block) and islands, the diagonal with fewer votes removed, both on a
+     * tie. Not in the reference; no parity target beyond the oracle. */
+    int vote;
 } depix_params;
 
 void depix_default_params(depix_params* p);
@@ -96,6 +103,11 @@ depix_status depix_resolve_trivial(uint8_t* d_graph, int w, int h, depix_stream 
  * reads the snapshot d_snapshot (the graph after trivial removal), writes the
  * resolved graph to d_out. The two buffers must not overlap. */
 depix_status depix_resolve_heuristics(const uint8_t* d_snapshot, int w, int h, uint8_t* d_out, depix_stream s);
+
+/* The same with the weighted vote (depix_params.vote = 1) instead of the
+ * reference's ordered tests. No counterpart in the reference. */
+depix_status depix_resolve_heuristics_vote(const uint8_t* d_snapshot, int w, int h, uint8_t* d_out,
+                                           depix_stream s);
 
 /* Reshaped cells (cells_Kernel, kernel.cu:192-213) in the reference's
  * 45-slot layout: d_diagram gets w*h*45 (x,y) float pairs, local cell

@@ -179,6 +179,87 @@ static int block_decision(const uint8_t* g, int w, int h, int i, int j)
     return seg2 < seg ? 0 : 1;
 }
 
+/* Pixels of the component of (si, sj) inside the 8x8 window whose lower-left
+ * pixel is (wi, wj), following set edge bits between window pixels only
+ * (breadth-first search). */
+static int window_component(const uint8_t* g, int w, int h, int wi, int wj, int si, int sj)
+{
+    int seen[8][8] = {{0}};
+    int qx[64], qy[64], head = 0, tail = 0;
+    seen[sj - wj][si - wi] = 1;
+    qx[tail] = si;
+    qy[tail++] = sj;
+    while (head < tail) {
+        int x = qx[head], y = qy[head++];
+        unsigned nd = gat(g, w, h, x, y);
+        for (int e = 0; e < 8; e++) {
+            if (!bit_of(nd, e)) continue;
+            int nx = x + DI[e], ny = y + DJ[e];
+            if (nx < wi || ny < wj || nx >= wi + 8 || ny >= wj + 8 || seen[ny - wj][nx - wi]) continue;
+            seen[ny - wj][nx - wi] = 1;
+            qx[tail] = nx;
+            qy[tail++] = ny;
+        }
+    }
+    return tail;
+}
+
+/* Not in the reference: the weighted vote of Kopf and Lischinski,
+ * "Depixelizing Pixel Art" (SIGGRAPH 2011), section 3.2, for the block whose
+ * lower-left node is (i, j). Votes go to the diagonal to keep: curves by the
+ * difference of the curve lengths (the walks of block_decision), sparse
+ * pixels by the difference of the two diagonals' component sizes inside the
+ * 8x8 window centred on the block (the smaller component's diagonal is
+ * kept), islands 5 for a diagonal with an end that has no other edge.
+ * Returns bit 0 to remove "/" (bits 2/5), bit 1 to remove "\" (bits 0/7);
+ * a tie removes both. */
+static int vote_decision(const uint8_t* g, int w, int h, int i, int j)
+{
+    unsigned n1 = gat(g, w, h, i, j), n2 = gat(g, w, h, i, j + 1);
+    unsigned n3 = gat(g, w, h, i + 1, j), n4 = gat(g, w, h, i + 1, j + 1);
+    int keep_slash = 0, keep_back = 0;
+    int seg = 0, seg2 = 0;
+    walk_len(g, w, h, i, j, 2, &seg);
+    walk_len(g, w, h, i + 1, j + 1, 5, &seg);
+    walk_len(g, w, h, i + 1, j, 0, &seg2);
+    walk_len(g, w, h, i, j + 1, 7, &seg2);
+    if (seg > seg2) keep_slash += seg - seg2;
+    else keep_back += seg2 - seg;
+    if (others(n1, 2, 0) == 0 || others(n4, 5, 0) == 0) keep_slash += 5;
+    if (others(n3, 0, 0) == 0 || others(n2, 7, 0) == 0) keep_back += 5;
+    int a = window_component(g, w, h, i - 3, j - 3, i, j);
+    int b = window_component(g, w, h, i - 3, j - 3, i, j + 1);
+    if (a < b) keep_slash += b - a;
+    else keep_back += a - b;
+    if (keep_slash > keep_back) return 2;
+    if (keep_back > keep_slash) return 1;
+    return 3;
+}
+
+/* The heuristics pass with the vote: each node of a crossing block clears
+ * its own bit of every diagonal the vote removes. */
+void orc_heuristics_vote(const uint8_t* snap, int w, int h, uint8_t* out)
+{
+    for (int j = 0; j < h; j++)
+        for (int i = 0; i < w; i++) {
+            unsigned c = gat(snap, w, h, i, j);
+            unsigned o = c;
+            if (bit_of(gat(snap, w, h, i - 1, j), 2) && bit_of(gat(snap, w, h, i - 1, j + 1), 7) && bit_of(c, 0) &&
+                bit_of(gat(snap, w, h, i, j + 1), 5))
+                if (vote_decision(snap, w, h, i - 1, j) & 2) o &= ~1u;
+            if (bit_of(gat(snap, w, h, i - 1, j - 1), 2) && bit_of(gat(snap, w, h, i - 1, j), 7) &&
+                bit_of(gat(snap, w, h, i, j - 1), 0) && bit_of(c, 5))
+                if (vote_decision(snap, w, h, i - 1, j - 1) & 1) o &= ~32u;
+            if (bit_of(gat(snap, w, h, i, j - 1), 2) && bit_of(c, 7) && bit_of(gat(snap, w, h, i + 1, j - 1), 0) &&
+                bit_of(gat(snap, w, h, i + 1, j), 5))
+                if (vote_decision(snap, w, h, i, j - 1) & 2) o &= ~128u;
+            if (bit_of(c, 2) && bit_of(gat(snap, w, h, i, j + 1), 7) && bit_of(gat(snap, w, h, i + 1, j), 0) &&
+                bit_of(gat(snap, w, h, i + 1, j + 1), 5))
+                if (vote_decision(snap, w, h, i, j) & 1) o &= ~4u;
+            out[j * w + i] = (uint8_t)o;
+        }
+}
+
 /* Heuristic crossing resolution (crossCheck_Heuristics,
  * graph_functions.cu:1433-1518): for each of the four 2x2 blocks around a
  * node in which both diagonals survive in the snapshot, the node clears its

@@ -47,6 +47,7 @@ def lib():
                                 ctypes.c_int, _u8p]
         L.orc_trivial.argtypes = [_u8p, ctypes.c_int, ctypes.c_int]
         L.orc_heuristics.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u8p]
+        L.orc_heuristics_vote.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_hull_table.argtypes = [_i32p, _i8p]
         L.orc_raster.argtypes = [_f32p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_label_cc.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _i32p]
@@ -96,17 +97,24 @@ def yuv_word(b0, b1, b2) -> int:
     return int(lib().orc_yuv_word(b0, b1, b2))
 
 
-def graph(bgr, w, h, ws, tr=(48, 7, 6)):
-    """Similarity graph, then trivial and heuristic resolution: returns
+def graph(bgr, w, h, ws, tr=(48, 7, 6), vote=False):
+    """Similarity graph, then trivial and heuristic resolution (the
+    reference's ordered tests, or the weighted vote): returns
     (raw, after_trivial, resolved)."""
     bgr = np.ascontiguousarray(bgr, np.uint8)
     raw = np.zeros(w * h, np.uint8)
     lib().orc_graph(bgr, w, h, ws, tr[0], tr[1], tr[2], raw)
     triv = raw.copy()
     lib().orc_trivial(triv, w, h)
+    return raw, triv, heuristics(triv, w, h, vote)
+
+
+def heuristics(snap, w, h, vote=False):
+    """Heuristic resolution of a graph after trivial removal."""
     res = np.zeros(w * h, np.uint8)
-    lib().orc_heuristics(triv, w, h, res)
-    return raw, triv, res
+    fn = lib().orc_heuristics_vote if vote else lib().orc_heuristics
+    fn(np.ascontiguousarray(snap, np.uint8).reshape(-1), w, h, res)
+    return res
 
 
 def hull_table():

@@ -148,6 +148,7 @@ depix_status check_params(const depix_params* p)
     if (!p) return arg_fail("params pointer is NULL");
     if (p->scale < 1 || p->scale > 64) return arg_fail("scale must be in 1..64");
     if (p->tr_y < 0 || p->tr_u < 0 || p->tr_v < 0) return arg_fail("thresholds must be >= 0");
+    if (p->vote != 0 && p->vote != 1) return arg_fail("vote must be 0 or 1");
     return DEPIX_OK;
 }
 
@@ -189,6 +190,7 @@ void depix_default_params(depix_params* p)
     p->tr_v = 6;
     p->subdivide = 1;
     p->scale = 4;
+    p->vote = 0;
 }
 
 const char* depix_status_string(depix_status s)
@@ -247,6 +249,16 @@ depix_status depix_resolve_heuristics(const uint8_t* d_snapshot, int w, int h, u
     if (!d_snapshot || !d_out) return arg_fail("graph pointer is NULL");
     if (d_snapshot == d_out) return arg_fail("snapshot and output must be distinct buffers");
     GraphBatch b{d_snapshot, d_out, 0, w, h};
+    DEPIX_CK(launch_heuristics(b, 1, S(s)));
+    return DEPIX_OK;
+}
+
+depix_status depix_resolve_heuristics_vote(const uint8_t* d_snapshot, int w, int h, uint8_t* d_out, depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (!d_snapshot || !d_out) return arg_fail("graph pointer is NULL");
+    if (d_snapshot == d_out) return arg_fail("snapshot and output must be distinct buffers");
+    GraphBatch b{d_snapshot, d_out, 0, w, h, 1};
     DEPIX_CK(launch_heuristics(b, 1, S(s)));
     return DEPIX_OK;
 }
@@ -495,7 +507,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         {
             // with labels, each heuristics tile also makes its local labels
             StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
-            GraphBatch hb{ctx->graph_a, ctx->graph_b, px, w[0], h[0]};
+            GraphBatch hb{ctx->graph_a, ctx->graph_b, px, w[0], h[0], p->vote};
             if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, n, d_labels, s));
             else DEPIX_CK(launch_heuristics(hb, n, s));
         }
@@ -520,7 +532,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         DEPIX_TRY(ensure_tables(s));
         DEPIX_TRY(scale_table(p->scale, s, &lut));
         const QueueCall c{n, w, h, in_offset, out_offset, d_img, d_out, d_labels, thr, p->subdivide, p->scale,
-                          lut, ctx->graph_a, ctx->graph_b};
+                          p->vote, lut, ctx->graph_a, ctx->graph_b};
         DEPIX_TRY(queue_prepare(ctx->queue, c, s));
         if (!ctx->timing) return queue_launch_graph(ctx->queue, s);
         DEPIX_TRY(queue_reset(ctx->queue, s));
@@ -545,7 +557,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
         }
         {
             StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
-            GraphBatch hb{ctx->graph_a + goff, ctx->graph_b + goff, 0, w[k], h[k]};
+            GraphBatch hb{ctx->graph_a + goff, ctx->graph_b + goff, 0, w[k], h[k], p->vote};
             if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, 1, d_labels + loff, s));
             else DEPIX_CK(launch_heuristics(hb, 1, s));
         }
@@ -763,7 +775,7 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
     }
     {
         StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
-        GraphBatch hb{ctx->graph_a, resolved, 0, w, h};
+        GraphBatch hb{ctx->graph_a, resolved, 0, w, h, p->vote};
         if (d_labels) DEPIX_CK(launch_heuristics_labels(hb, 1, d_labels, s));
         else DEPIX_CK(launch_heuristics(hb, 1, s));
     }
@@ -894,7 +906,7 @@ depix_status compat_run(void* pos, void* colorPos, char* img_data, int w, int h,
     DEPIX_CK(cudaMemcpyAsync(c.img, img_data, ib, cudaMemcpyHostToDevice, s));
     FrameBatch gb{c.img, 0, c.g0, 0, w, h, ws, DEPIX_LAYOUT_BGR};
     DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
-    GraphBatch hb{c.g0, c.g1, 0, w, h};
+    GraphBatch hb{c.g0, c.g1, 0, w, h, p->vote};
     DEPIX_CK(launch_heuristics(hb, 1, s));
     DEPIX_CK(launch_cells(c.g1, w, h, c.diag, c.ec, s));
     if (subdivide) {

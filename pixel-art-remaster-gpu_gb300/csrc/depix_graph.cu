@@ -223,6 +223,79 @@ __device__ bool block_decision(const SnapTile& t, int i, int j)
     return !(seg2 < seg);
 }
 
+// Block decision codes: bit 0 a crossing, bit 1 remove "/" (bits 2/5),
+// bit 2 remove "\" (bits 0/7).
+constexpr unsigned kDecCross = 1, kDecSlash = 2, kDecBack = 4;
+
+// Size of the component of `seed` in an 8x8 window whose bit r*8+c is the
+// pixel in window row r, column c; m[e] holds the pixels with edge e. The
+// fill follows the edges inside the window only (a move off the window's
+// columns is masked, one off its rows shifts out).
+__device__ __forceinline__ int window_component(const uint64_t (&m)[8], uint64_t seed)
+{
+    constexpr uint64_t kCol0 = 0x0101010101010101ull, kCol7 = 0x8080808080808080ull;
+    uint64_t c = seed, prev;
+    do {
+        prev = c;
+        c |= ((prev & m[0]) << 7) & ~kCol7; // (-1, +1)
+        c |= (prev & m[1]) << 8;            // ( 0, +1)
+        c |= ((prev & m[2]) << 9) & ~kCol0; // (+1, +1)
+        c |= ((prev & m[3]) >> 1) & ~kCol7; // (-1,  0)
+        c |= ((prev & m[4]) << 1) & ~kCol0; // (+1,  0)
+        c |= ((prev & m[5]) >> 9) & ~kCol7; // (-1, -1)
+        c |= (prev & m[6]) >> 8;            // ( 0, -1)
+        c |= ((prev & m[7]) >> 7) & ~kCol0; // (+1, -1)
+    } while (c != prev);
+    return __popcll(c);
+}
+
+// Weighted vote of the three heuristics of Kopf and Lischinski,
+// "Depixelizing Pixel Art" (SIGGRAPH 2011), section 3.2, for the block whose
+// lower-left node is (i, j); not in the reference, which decides by the
+// ordered tests of block_decision. Each heuristic votes for the diagonal to
+// keep: curves by the difference of the two curve lengths (the same walks as
+// block_decision), sparse pixels by the difference of the sizes of the two
+// diagonals' components inside the 8x8 window centred on the block (the
+// sparser one is kept), islands with weight 5 for a diagonal whose removal
+// would leave one of its ends without edges. The diagonal with fewer votes
+// is removed; a tie removes both.
+__device__ unsigned vote_decision(const uint8_t (*s)[kHRW], int ox, int oy, int i, int j)
+{
+    const SnapTile t{s, ox, oy};
+    unsigned n1 = t.at(i, j), n2 = t.at(i, j + 1), n3 = t.at(i + 1, j), n4 = t.at(i + 1, j + 1);
+    int dummy;
+    int o1 = others(n1, 2, dummy), o4 = others(n4, 5, dummy), o3 = others(n3, 0, dummy), o2 = others(n2, 7, dummy);
+    int keep_slash = 0, keep_back = 0;
+    int seg = 0, seg2 = 0;
+    walk_len(t, i, j, 2, seg);
+    walk_len(t, i + 1, j + 1, 5, seg);
+    walk_len(t, i + 1, j, 0, seg2);
+    walk_len(t, i, j + 1, 7, seg2);
+    if (seg > seg2) keep_slash += seg - seg2;
+    else keep_back += seg2 - seg;
+    if (o1 == 0 || o4 == 0) keep_slash += 5;
+    if (o3 == 0 || o2 == 0) keep_back += 5;
+    // window columns i-3 .. i+4, rows j-3 .. j+4 (inside the snapshot halo)
+    uint64_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int r = 0; r < 8; r++) {
+        const uint8_t* row = &s[j - 3 + r - oy][i - 3 - ox];
+        for (int c = 0; c < 8; c++) {
+            const unsigned nd = row[c];
+            const uint64_t bit = 1ull << (r * 8 + c);
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+                if (nd >> e & 1u) m[e] |= bit;
+        }
+    }
+    // i1 = (i, j) is window bit 27 (with i4 on "/"), i2 = (i, j + 1) bit 35
+    const int size_slash = window_component(m, 1ull << 27), size_back = window_component(m, 1ull << 35);
+    if (size_slash < size_back) keep_slash += size_back - size_slash;
+    else keep_back += size_slash - size_back;
+    if (keep_slash > keep_back) return kDecCross | kDecBack;
+    if (keep_back > keep_slash) return kDecCross | kDecSlash;
+    return kDecCross | kDecSlash | kDecBack;
+}
+
 template <int TW, int TH>
 __device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t* L, int w, int h, int x0, int y0);
 
@@ -230,7 +303,7 @@ __device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t
 // component labels too (union-find over the resolved bytes, still in shared
 // memory), which leaves the label stage only the merge across tile borders
 // and the flattening.
-template <bool TMA = false>
+template <bool TMA = false, bool VOTE = false>
 __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* out, int w, int h, int x0, int y0,
                                                 int32_t* L = nullptr, const CUtensorMap* map = nullptr,
                                                 int frame = 0)
@@ -270,19 +343,21 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
     }
     SnapTile t{s, ox, oy};
     // each 2x2 block touching the tile decided once (the four corner nodes
-    // each clear their own bit of it): bit 0 a crossing, bit 1 the decision
-    // (true removes "/", false "\"); blocks reaching outside the image read
-    // the zero halo and are never crossings
+    // each clear their own bit of it), as a kDec* code; blocks reaching
+    // outside the image read the zero halo and are never crossings
     __shared__ uint8_t dec[kHTH + 1][kHTW + 1];
     __syncthreads();
     for (int k = threadIdx.x; k < (kHTW + 1) * (kHTH + 1); k += blockDim.x) {
         const int bx = k % (kHTW + 1), by = k / (kHTW + 1);
         const int bi = x0 - 1 + bx, bj = y0 - 1 + by;
-        uint8_t d = 0;
+        unsigned d = 0;
         if (bitof(t.at(bi, bj), 2) && bitof(t.at(bi, bj + 1), 7) && bitof(t.at(bi + 1, bj), 0) &&
             bitof(t.at(bi + 1, bj + 1), 5))
-            d = 1 | (block_decision(t, bi, bj) ? 2 : 0);
-        dec[by][bx] = d;
+        {
+            if constexpr (VOTE) d = vote_decision(s, ox, oy, bi, bj);
+            else d = kDecCross | (block_decision(t, bi, bj) ? kDecSlash : kDecBack);
+        }
+        dec[by][bx] = (uint8_t)d;
     }
     __syncthreads();
     __shared__ uint8_t res[kHTW * kHTH];
@@ -297,10 +372,10 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
         // the node is the lower-right corner of block (i-1, j), the upper-right
         // of (i-1, j-1), the upper-left of (i, j-1), the lower-left of (i, j)
         const unsigned a = dec[ty + 1][tx], b = dec[ty][tx], c = dec[ty][tx + 1], d = dec[ty + 1][tx + 1];
-        if (a == 1) o &= ~1u;
-        if (b == 3) o &= ~32u;
-        if (c == 1) o &= ~128u;
-        if (d == 3) o &= ~4u;
+        if (a & kDecBack) o &= ~1u;
+        if (b & kDecSlash) o &= ~32u;
+        if (c & kDecBack) o &= ~128u;
+        if (d & kDecSlash) o &= ~4u;
         out[(size_t)j * w + i] = (uint8_t)o;
         res[k] = (uint8_t)(o & inside_mask(i, j, w, h));
     }
@@ -312,28 +387,33 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
     }
 }
 
+// VOTE: the weighted vote instead of the reference's ordered tests
+template <bool VOTE>
 __global__ void __launch_bounds__(256) k_heuristics(GraphBatch b)
 {
     const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
     uint8_t* out = b.out + b.frame_stride * blockIdx.z;
-    heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH);
+    heuristics_tile<false, VOTE>(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH);
 }
 
+template <bool VOTE>
 __global__ void __launch_bounds__(256) k_heuristics_labels(GraphBatch b, int32_t* L)
 {
     const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
     uint8_t* out = b.out + b.frame_stride * blockIdx.z;
-    heuristics_tile(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH, L + b.frame_stride * blockIdx.z);
+    heuristics_tile<false, VOTE>(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH,
+                                 L + b.frame_stride * blockIdx.z);
 }
 
 // the same with the graph windows by TMA (width and frame stride multiples of
 // 16 bytes, 16-byte aligned base); L may be NULL
+template <bool VOTE>
 __global__ void __launch_bounds__(256) k_heuristics_tma(GraphBatch b, int32_t* L, const __grid_constant__ CUtensorMap map)
 {
     const uint8_t* snap = b.snap + b.frame_stride * blockIdx.z;
     uint8_t* out = b.out + b.frame_stride * blockIdx.z;
-    heuristics_tile<true>(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH,
-                          L ? L + b.frame_stride * blockIdx.z : nullptr, &map, (int)blockIdx.z);
+    heuristics_tile<true, VOTE>(snap, out, b.w, b.h, blockIdx.x * kHTW, blockIdx.y * kHTH,
+                                L ? L + b.frame_stride * blockIdx.z : nullptr, &map, (int)blockIdx.z);
 }
 
 // -------------------------------------------------- component labelling
@@ -563,6 +643,7 @@ __global__ void __launch_bounds__(256) k_graph_queue(QueueBatch q)
     });
 }
 
+template <bool VOTE>
 __global__ void __launch_bounds__(256) k_heur_queue(QueueBatch q)
 {
     const QueueHeader* H = q.hdr;
@@ -572,8 +653,8 @@ __global__ void __launch_bounds__(256) k_heur_queue(QueueBatch q)
         const int f = queue_frame(base, n, (uint32_t)t);
         const QueueFrame fr = H->frames[f];
         const int lt = t - (int)base[f], tx = (fr.w + kHTW - 1) / kHTW;
-        heuristics_tile(q.graph_a + fr.px_off, q.graph_b + fr.px_off, fr.w, fr.h, (lt % tx) * kHTW,
-                        (lt / tx) * kHTH, H->labels ? H->labels + fr.px_off : nullptr);
+        heuristics_tile<false, VOTE>(q.graph_a + fr.px_off, q.graph_b + fr.px_off, fr.w, fr.h, (lt % tx) * kHTW,
+                                     (lt / tx) * kHTH, H->labels ? H->labels + fr.px_off : nullptr);
     });
 }
 
@@ -619,7 +700,8 @@ cudaError_t queue_graph(const QueueBatch& q, int blocks, cudaStream_t s)
 
 cudaError_t queue_heuristics(const QueueBatch& q, int blocks, cudaStream_t s)
 {
-    k_heur_queue<<<blocks, 256, 0, s>>>(q);
+    if (q.vote) k_heur_queue<true><<<blocks, 256, 0, s>>>(q);
+    else k_heur_queue<false><<<blocks, 256, 0, s>>>(q);
     return cudaGetLastError();
 }
 
@@ -647,7 +729,7 @@ int queue_blocks_per_sm(int stage, const QueueBatch& q)
 {
     switch (stage) {
     case QS_GRAPH: return occupancy(k_graph_queue, 256);
-    case QS_HEUR: return occupancy(k_heur_queue, 256);
+    case QS_HEUR: return q.vote ? occupancy(k_heur_queue<true>, 256) : occupancy(k_heur_queue<false>, 256);
     case QS_LABEL: return occupancy(k_label_flatten_queue, 256);
     default: return queue_raster_blocks_per_sm(q);
     }
@@ -702,10 +784,11 @@ cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s)
 {
     dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
     CUtensorMap map;
-    if (u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map))
-        k_heuristics_tma<<<grid, 256, 0, s>>>(b, nullptr, map);
-    else
-        k_heuristics<<<grid, 256, 0, s>>>(b);
+    const bool tma = u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map);
+    if (tma && b.vote) k_heuristics_tma<true><<<grid, 256, 0, s>>>(b, nullptr, map);
+    else if (tma) k_heuristics_tma<false><<<grid, 256, 0, s>>>(b, nullptr, map);
+    else if (b.vote) k_heuristics<true><<<grid, 256, 0, s>>>(b);
+    else k_heuristics<false><<<grid, 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -713,10 +796,11 @@ cudaError_t launch_heuristics_labels(const GraphBatch& b, int nframes, int32_t* 
 {
     dim3 grid((b.w + kHTW - 1) / kHTW, (b.h + kHTH - 1) / kHTH, nframes);
     CUtensorMap map;
-    if (u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map))
-        k_heuristics_tma<<<grid, 256, 0, s>>>(b, labels, map);
-    else
-        k_heuristics_labels<<<grid, 256, 0, s>>>(b, labels);
+    const bool tma = u8_tensor_map(b.snap, b.w, b.h, b.frame_stride, nframes, kHRW, kHRH, &map);
+    if (tma && b.vote) k_heuristics_tma<true><<<grid, 256, 0, s>>>(b, labels, map);
+    else if (tma) k_heuristics_tma<false><<<grid, 256, 0, s>>>(b, labels, map);
+    else if (b.vote) k_heuristics_labels<true><<<grid, 256, 0, s>>>(b, labels);
+    else k_heuristics_labels<false><<<grid, 256, 0, s>>>(b, labels);
     return cudaGetLastError();
 }
 

@@ -35,6 +35,7 @@ struct GraphBatch {
     uint8_t* out;
     size_t frame_stride;
     int w, h;
+    int vote = 0; // heuristics: 0 the reference's ordered tests, 1 the weighted vote
 };
 
 // Raster of equal-size frames.
@@ -94,6 +95,7 @@ struct QueueBatch {
     int gran[QS_COUNT];   // tiles pulled per counter step, per stage
     int rtw, rth;         // raster tile (cells); 0, 0: each frame in its own shape
     int rbase;            // first raster prefix: QS_RASTER (one shape for all) or kQMixedBase
+    int vote;             // heuristics by the weighted vote (GraphBatch::vote)
 };
 
 // tiles of a frame per stage; the raster has three tile shapes, each with its
@@ -124,6 +126,7 @@ struct QueueCall {
     int32_t* labels;      // NULL: no label stage
     uint32_t thr;
     int subdivide, scale;
+    int vote;
     const uint32_t* lut;
     uint8_t* graph_a;
     uint8_t* graph_b;

@@ -43,10 +43,10 @@ int log2_floor(uint64_t x)
 }
 
 // Graph cache key: everything a captured graph bakes in besides the context.
-uint64_t graph_key(int scale, bool labels, const QueueShape& sh)
+uint64_t graph_key(int scale, bool labels, int vote, const QueueShape& sh)
 {
     const int shape = sh.rtw == 0 ? 3 : raster_shape_index(sh.rtw, sh.rth);
-    uint64_t k = (uint64_t)scale | (uint64_t)labels << 8 | (uint64_t)shape << 9;
+    uint64_t k = (uint64_t)scale | (uint64_t)labels << 8 | (uint64_t)shape << 9 | (uint64_t)vote << 28;
     for (int st = 0; st < QS_COUNT; st++) k |= (uint64_t)log2_floor((uint64_t)sh.gran[st]) << (12 + 4 * st);
     return k;
 }
@@ -109,7 +109,7 @@ public:
     {
         const uint64_t key = stage == QS_RASTER
                                  ? (uint64_t)(4 + raster_shape_index(b.rtw, b.rth)) | (uint64_t)b.scale << 8
-                                 : (uint64_t)stage;
+                                 : (uint64_t)stage | (uint64_t)b.vote << 16;
         auto it = occ.find(key);
         if (it != occ.end()) return it->second;
         const int v = queue_blocks_per_sm(stage, b);
@@ -293,7 +293,7 @@ depix_status QueueRunner::tune(cudaStream_t s, QueueShape* out)
 // reset and the stage kernels, captured once on a private stream.
 depix_status QueueRunner::graph_for(cudaGraphExec_t* out)
 {
-    const uint64_t key = graph_key(q.scale, labels, shape);
+    const uint64_t key = graph_key(q.scale, labels, q.vote, shape);
     auto it = graphs.find(key);
     if (it != graphs.end()) {
         *out = it->second;
@@ -404,14 +404,14 @@ depix_status queue_prepare(QueueRunner* r, const QueueCall& c, cudaStream_t s)
 
     r->labels = c.labels != nullptr;
     r->q = QueueBatch{reinterpret_cast<const QueueHeader*>(r->d_desc), r->d_counters, c.graph_a, c.graph_b, c.lut,
-                      c.scale, {1, 1, 1, 1}, 32, 32, QS_RASTER};
+                      c.scale, {1, 1, 1, 1}, 32, 32, QS_RASTER, c.vote};
     if (r->forced) {
         r->shape = r->force;
         return DEPIX_OK;
     }
     // size bucket: frame count and mean frame size (powers of two), scale, labels
     const uint64_t bucket = (uint64_t)log2_floor((uint64_t)n) | (uint64_t)log2_floor(px / (uint64_t)n) << 8 |
-                            (uint64_t)c.scale << 16 | (uint64_t)r->labels << 24;
+                            (uint64_t)c.scale << 16 | (uint64_t)r->labels << 24 | (uint64_t)c.vote << 25;
     auto it = r->tuned.find(bucket);
     if (it != r->tuned.end()) {
         r->shape = it->second;

@@ -1222,6 +1222,10 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
         set_last_error("refine scale must be in 1..12");
         return DEPIX_ERR_INVALID_ARG;
     }
+    if (p->vote != 0 && p->vote != 1) {
+        set_last_error("vote must be 0 or 1");
+        return DEPIX_ERR_INVALID_ARG;
+    }
     if (layout == DEPIX_LAYOUT_RGBA ? (widthstep < 4 * w || (widthstep & 3)) : (layout != DEPIX_LAYOUT_BGR || widthstep < 3 * w)) {
         set_last_error("refine setup: bad layout or widthstep");
         return DEPIX_ERR_INVALID_ARG;
@@ -1235,7 +1239,7 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
         RF_CK(r->own_snap.reserve(n));
         const FrameBatch fb{d_img, 0, r->own_snap.p, 0, w, h, widthstep, (int)layout};
         RF_CK(launch_graph(fb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
-        RF_CK(launch_heuristics(GraphBatch{r->own_snap.p, r->own_graph.p, 0, w, h}, 1, s));
+        RF_CK(launch_heuristics(GraphBatch{r->own_snap.p, r->own_graph.p, 0, w, h, p->vote}, 1, s));
         d_graph = r->own_graph.p;
     }
     Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, r->box.p,

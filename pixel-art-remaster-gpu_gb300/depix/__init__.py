@@ -26,7 +26,7 @@ class DepixError(RuntimeError):
 
 class Params(ctypes.Structure):
     _fields_ = [("tr_y", ctypes.c_int), ("tr_u", ctypes.c_int), ("tr_v", ctypes.c_int),
-                ("subdivide", ctypes.c_int), ("scale", ctypes.c_int)]
+                ("subdivide", ctypes.c_int), ("scale", ctypes.c_int), ("vote", ctypes.c_int)]
 
 
 class RefineParams(ctypes.Structure):
@@ -38,8 +38,11 @@ def refine_params(w_curvature=1.0, w_deviation=0.25, w_coverage=1.0, sigma=0.5, 
     return RefineParams(w_curvature, w_deviation, w_coverage, sigma, lr, steps)
 
 
-def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4) -> Params:
-    return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale)
+def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4, vote=False) -> Params:
+    """Frame-path parameters; vote=True resolves ambiguous crossings by the
+    weighted vote (curves, sparse pixels, islands) instead of the
+    reference's ordered tests."""
+    return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale, int(bool(vote)))
 
 
 _lib = None
@@ -69,6 +72,7 @@ def lib():
         _sig(L, "depix_graph", [_vp, _i, _i, _i, _i, P, _i, _vp, _vp])
         _sig(L, "depix_resolve_trivial", [_vp, _i, _i, _vp])
         _sig(L, "depix_resolve_heuristics", [_vp, _i, _i, _vp, _vp])
+        _sig(L, "depix_resolve_heuristics_vote", [_vp, _i, _i, _vp, _vp])
         _sig(L, "depix_cells", [_vp, _i, _i, _vp, _vp, _vp])
         _sig(L, "depix_subdivide", [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp])
         _sig(L, "depix_triangulate", [_vp, _vp, _i, _i, _vp])
@@ -148,8 +152,13 @@ def resolve_trivial(g, w, h, stream=None):
     _check(lib().depix_resolve_trivial(ptr(g), w, h, stream_ptr(stream)), "depix_resolve_trivial")
 
 
-def resolve_heuristics(snap, w, h, out, stream=None):
-    _check(lib().depix_resolve_heuristics(ptr(snap), w, h, ptr(out), stream_ptr(stream)), "depix_resolve_heuristics")
+def resolve_heuristics(snap, w, h, out, stream=None, vote=False):
+    if vote:
+        _check(lib().depix_resolve_heuristics_vote(ptr(snap), w, h, ptr(out), stream_ptr(stream)),
+               "depix_resolve_heuristics_vote")
+    else:
+        _check(lib().depix_resolve_heuristics(ptr(snap), w, h, ptr(out), stream_ptr(stream)),
+               "depix_resolve_heuristics")
 
 
 def cells(g, w, h, diagram, ec, stream=None):

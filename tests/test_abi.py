@@ -56,6 +56,12 @@ def test_bad_arguments_are_rejected_before_cuda(L):
                           ctypes.c_void_p(16), None) == 1
     # aliasing snapshot and output
     assert L.depix_resolve_heuristics(ctypes.c_void_p(16), 4, 4, ctypes.c_void_p(16), None) == 1
+    assert L.depix_resolve_heuristics_vote(ctypes.c_void_p(16), 4, 4, ctypes.c_void_p(16), None) == 1
+    # heuristics decision other than 0 / 1
+    bad = depix.params()
+    bad.vote = 2
+    assert L.depix_graph(ctypes.c_void_p(16), 4, 4, 16, 1, ctypes.byref(bad), 1, ctypes.c_void_p(16), None) == 1
+    assert b"vote" in L.depix_last_error()
     # empty context
     h = ctypes.c_void_p()
     assert L.depix_context_create(ctypes.byref(h), 0, 1) == 1
@@ -68,4 +74,4 @@ def test_default_params(L):
     import depix
     p = depix.Params()
     L.depix_default_params(ctypes.byref(p))
-    assert (p.tr_y, p.tr_u, p.tr_v, p.subdivide, p.scale) == (48, 7, 6, 1, 4)
+    assert (p.tr_y, p.tr_u, p.tr_v, p.subdivide, p.scale, p.vote) == (48, 7, 6, 1, 4, 0)
