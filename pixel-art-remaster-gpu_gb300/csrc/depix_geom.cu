@@ -646,12 +646,16 @@ struct MaskTile {
     uint8_t spill[GN]; // bit e: the polygon reaches into the open square of neighbour e
     uint8_t live[GN];  // the cell exists (inside the image)
     uint16_t list[GN]; // subdivided cells of the tile, then the blocks that need owner resolution
-    uint16_t rep[GN];  // per subdivided cell: the list entry whose polygon (and mask) it shares
-    uint16_t reps[GN]; // list entries that make a mask
-    unsigned long long table[kPolyTable]; // distinct polygons: hash tag | (list entry + 1), 0 empty
+    uint16_t rep[GN];  // per subdivided cell: the list entry whose key, then whose polygon, it shares
+    uint16_t reps[GN]; // list entries that build a polygon (one per distinct key)
+    // distinct keys (first half), then distinct polygons (second half): hash
+    // tag | (list entry + 1), 0 empty; the first half later holds the list
+    // entries that make a mask
+    unsigned long long table[kPolyTable];
     int count;
     int slow;          // blocks in list for the owner-resolution pass
     int nreps;
+    int nmakers;
 };
 
 __device__ __forceinline__ uint32_t rgba_of(uint32_t p)
@@ -845,6 +849,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         M.count = 0;
         M.slow = 0;
         M.nreps = 0;
+        M.nmakers = 0;
     }
     for (int k = threadIdx.x; k < kPolyTable; k += blockDim.x) M.table[k] = 0ull;
     if (!(TMA && graph_map)) {
@@ -917,76 +922,147 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
     }
     __syncthreads();
 
-    // ---- phase B2: subdivided cells, one per thread
+    // ---- phase B2: subdivided cells
+    // A cut polygon is a function of the 5x3 graph bytes around its cell and
+    // of the corner tests (tj) at the four cell corners, and its mask is a
+    // function of the polygon. So (B2a) each cell keys itself by those inputs
+    // and one cell per distinct key builds the polygon (B2b), one builder per
+    // distinct polygon makes the mask (B2c), and the others copy (B2d). Cells
+    // whose corner test goes through the reference's bounds test or linear
+    // addressing (image edges) build on their own.
     const int nlist = M.count;
-    for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
-        int k = M.list[q];
-        int lx = k % T::GW, ly = k / T::GW;
-        int ci = x0 - 1 + lx, cj = y0 - 1 + ly;
-        const int bx = lx + 2, by = ly + 2;
-        auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx + T::kGOff]; };
-        auto tj = [&](int px, int py) -> bool {
-            long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
-            long long index = (long long)cj * st + (long long)ci * 3;
+    auto cell_at = [&](int k, int& lx, int& ly, int& ci, int& cj, bool& border) {
+        lx = k % T::GW;
+        ly = k / T::GW;
+        ci = x0 - 1 + lx;
+        cj = y0 - 1 + ly;
+        const long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
+        const long long index = (long long)cj * st + (long long)ci * 3;
+        border = (index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1) || ci == 0 || ci == w - 1 ||
+                 cj >= h - 1;
+    };
+    // corner test at vertex (px, py) of the cell at tile position (lx, ly)
+    auto tj_of = [&](int lx, int ly, int ci, int cj, bool border, int px, int py) -> bool {
+        if (border) {
+            const long long st = LAYOUT == DEPIX_LAYOUT_BGR ? ws : ((3 * w + 3) & ~3);
+            const long long index = (long long)cj * st + (long long)ci * 3;
             if ((index - st - 1) < 0 || (index + w + 1) > ((long long)h * st - 1)) return true;
-            if (ci == 0 || ci == w - 1 || cj >= h - 1) return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
-            const int qx = lx + 1, qy = ly + 1;
-            auto C = [&](int dx, int dy) { return M.pix[qy + dy][qx + dx + 2]; };
-            if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
-            if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
-            if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
-            if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
-            return false;
-        };
-        Packed sp;
-        cell_polygon(Gs, tj, sp);
-        uint32_t* rows = masks + (size_t)k * F;
-        if (F < 10) { // no room to park the polygon: every cell makes its mask
-            M.spill[k] = (uint8_t)polygon_mask(sp, G, rows, 1);
-            continue;
+            return t_junction_global(img, w, h, ws, LAYOUT, ci, cj, px, py);
         }
-        // the mask depends on the polygon alone: one cell per distinct polygon
-        // of the tile makes it, the others copy
-        park_polygon(sp, rows);
-        __threadfence_block();
-        const uint64_t h = polygon_hash(sp);
-        const unsigned long long tag = h & ~0xFFFFull;
-        int slot = (int)(h >> 16) & (kPolyTable - 1), rep = -1;
-        for (int probe = 0; probe < kPolyProbes && rep < 0; probe++, slot = (slot + 1) & (kPolyTable - 1)) {
-            unsigned long long cur = M.table[slot];
+        const int qx = lx + 1, qy = ly + 1;
+        auto C = [&](int dx, int dy) { return M.pix[qy + dy][qx + dx + 2]; };
+        if (px == 0 && py == 0) return C(-1, 0) != C(-1, -1) || C(-1, -1) != C(0, -1);
+        if (px == kUnit && py == 0) return C(1, 0) != C(1, -1) || C(1, -1) != C(0, -1);
+        if (px == kUnit && py == kUnit) return C(0, 1) != C(1, 1) || C(1, 1) != C(1, 0);
+        if (px == 0 && py == kUnit) return C(-1, 1) != C(0, 1) || C(0, 1) != C(-1, 0);
+        return false;
+    };
+    // insert-or-find in one half of the table: the list entry whose parked
+    // words equal this entry's (same(rq)), or q when q took a free slot or
+    // the probes ran out
+    auto dedupe = [&](uint64_t hs, int half, int q, auto same) -> int {
+        const unsigned long long tag = hs & ~0xFFFFull;
+        constexpr int kHalf = kPolyTable / 2;
+        int slot = (int)(hs >> 16) & (kHalf - 1);
+        for (int probe = 0; probe < kPolyProbes; probe++, slot = (slot + 1) & (kHalf - 1)) {
+            unsigned long long* e = &M.table[half * kHalf + slot];
+            unsigned long long cur = *e;
             if (cur == 0ull) {
-                cur = atomicCAS(&M.table[slot], 0ull, tag | (unsigned long long)(q + 1));
-                if (cur == 0ull) {
-                    rep = q;
-                    break;
-                }
+                cur = atomicCAS(e, 0ull, tag | (unsigned long long)(q + 1));
+                if (cur == 0ull) return q;
             }
             if ((cur & ~0xFFFFull) == tag) {
                 const int rq = (int)(cur & 0xFFFFull) - 1;
-                Packed other;
-                unpark_polygon(masks + (size_t)M.list[rq] * F, other);
-                if (other.n == sp.n && other.x0 == sp.x0 && other.x1 == sp.x1 && other.y0 == sp.y0 &&
-                    other.y1 == sp.y1)
-                    rep = rq;
+                if (same(rq)) return rq;
             }
         }
-        if (rep < 0) rep = q;
+        return q;
+    };
+    // B2a
+    for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
+        const int k = M.list[q];
+        int lx, ly, ci, cj;
+        bool border;
+        cell_at(k, lx, ly, ci, cj, border);
+        const int bx = lx + 2, by = ly + 2;
+        uint32_t* rows = masks + (size_t)k * F;
+        if (F < 10) { // no room to park keys or polygons: every cell makes its mask
+            auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx + T::kGOff]; };
+            auto tj = [&](int px, int py) -> bool { return tj_of(lx, ly, ci, cj, border, px, py); };
+            Packed sp;
+            cell_polygon(Gs, tj, sp);
+            M.spill[k] = (uint8_t)polygon_mask(sp, G, rows, 1);
+            continue;
+        }
+        int rep = q;
+        if (!border) {
+            auto B = [&](int dx, int dy) -> uint32_t { return M.graph[by + dy][bx + dx + T::kGOff]; };
+            const uint32_t corners = (uint32_t)tj_of(lx, ly, ci, cj, false, 0, 0) |
+                                     (uint32_t)tj_of(lx, ly, ci, cj, false, kUnit, 0) << 1 |
+                                     (uint32_t)tj_of(lx, ly, ci, cj, false, kUnit, kUnit) << 2 |
+                                     (uint32_t)tj_of(lx, ly, ci, cj, false, 0, kUnit) << 3;
+            const uint32_t w0 = B(-2, -1) | B(-1, -1) << 8 | B(0, -1) << 16 | B(1, -1) << 24;
+            const uint32_t w1 = B(2, -1) | B(-2, 0) << 8 | B(-1, 0) << 16 | B(0, 0) << 24;
+            const uint32_t w2 = B(1, 0) | B(2, 0) << 8 | B(-2, 1) << 16 | B(-1, 1) << 24;
+            const uint32_t w3 = B(0, 1) | B(1, 1) << 8 | B(2, 1) << 16 | corners << 24;
+            rows[0] = w0;
+            rows[1] = w1;
+            rows[2] = w2;
+            rows[3] = w3;
+            __threadfence_block();
+            Packed kp;
+            kp.x0 = w0 | (uint64_t)w1 << 32;
+            kp.x1 = w2 | (uint64_t)w3 << 32;
+            kp.y0 = kp.y1 = 0;
+            kp.n = 0;
+            rep = dedupe(polygon_hash(kp), 0, q, [&](int rq) {
+                const uint32_t* o = masks + (size_t)M.list[rq] * F;
+                return o[0] == w0 && o[1] == w1 && o[2] == w2 && o[3] == w3;
+            });
+        }
         M.rep[q] = (uint16_t)rep;
         if (rep == q) M.reps[atomicAdd(&M.nreps, 1)] = (uint16_t)q;
     }
     __syncthreads();
     if (F >= 10) {
-        const int nreps = M.nreps;
-        for (int i = threadIdx.x; i < nreps; i += blockDim.x) {
-            const int k = M.list[M.reps[i]];
+        // B2b: one polygon per distinct key, parked in its cell's rows; the
+        // builder's rep becomes the builder whose polygon (and mask) it shares
+        const int nb = M.nreps;
+        uint16_t* makers = reinterpret_cast<uint16_t*>(M.table); // the key half, free now
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+            const int q = M.reps[i], k = M.list[q];
+            int lx, ly, ci, cj;
+            bool border;
+            cell_at(k, lx, ly, ci, cj, border);
+            const int bx = lx + 2, by = ly + 2;
+            auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx + T::kGOff]; };
+            auto tj = [&](int px, int py) -> bool { return tj_of(lx, ly, ci, cj, border, px, py); };
+            Packed sp;
+            cell_polygon(Gs, tj, sp);
+            park_polygon(sp, masks + (size_t)k * F);
+            __threadfence_block();
+            const int rp = dedupe(polygon_hash(sp), 1, q, [&](int rq) {
+                Packed o;
+                unpark_polygon(masks + (size_t)M.list[rq] * F, o);
+                return o.n == sp.n && o.x0 == sp.x0 && o.x1 == sp.x1 && o.y0 == sp.y0 && o.y1 == sp.y1;
+            });
+            M.rep[q] = (uint16_t)rp;
+            if (rp == q) makers[atomicAdd(&M.nmakers, 1)] = (uint16_t)q;
+        }
+        __syncthreads();
+        // B2c: the masks
+        const int nm = M.nmakers;
+        for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+            const int k = M.list[makers[i]];
             uint32_t* rows = masks + (size_t)k * F;
             Packed sp;
             unpark_polygon(rows, sp);
             M.spill[k] = (uint8_t)polygon_mask(sp, G, rows, 1);
         }
         __syncthreads();
+        // B2d: copies (key rep -> its polygon's mask maker)
         for (int q = threadIdx.x; q < nlist; q += blockDim.x) {
-            const int rq = M.rep[q];
+            const int rq = M.rep[M.rep[q]];
             if (rq == q) continue;
             const int k = M.list[q], rk = M.list[rq];
             const uint32_t* src = masks + (size_t)rk * F;
