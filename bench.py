@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-stream", action="store_true")
     ap.add_argument("--no-vote", action="store_true")
+    ap.add_argument("--no-walks", action="store_true")
     ap.add_argument("--stream-frames", type=int, default=512)
     return ap.parse_args()
 
@@ -310,6 +311,8 @@ def run_ours(args, rank, world, local_rank):
         vote = {"frames_per_s": round(B * vsteps / (vms / 1e3), 1), "ms_per_step": round(vms / vsteps, 4),
                 "steps": vsteps, "stage_ms_per_step": {k: round(v[0] / max(v[2], 1), 4) for k, v in vst.items()}}
 
+    walks = None if args.no_walks else run_walks(args, dev, stream, d_in, cpu=(rank == 0 and world == 1 and not args.no_cpu))
+
     sprites = None if args.no_sprites else run_sprites(args, dev, stream)
     refine = None if args.no_refine else run_refine(args, dev, stream, cpu=(rank == 0 and world == 1 and not args.no_cpu))
     stream_leg = None if args.no_stream else run_stream(args, dev, stream)
@@ -330,8 +333,65 @@ def run_ours(args, rank, world, local_rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
-                "refine": refine, "stream": stream_leg, "vote": vote}
+                "refine": refine, "stream": stream_leg, "vote": vote, "border_walks": walks}
         print(json.dumps(line))
+
+
+def run_walks(args, dev, stream, d_in, cpu):
+    """Border walks (the spline export's input) of a batch of resolved
+    graphs: the graphs of the distinct frames tiled to the batch size, one
+    warp per frame; CUDA-event time per batch."""
+    import numpy as np
+    import torch
+    import depix
+    B, N = args.batch, W * H
+    p = depix.params(48, 7, 6, True, SCALE)
+    fused = torch.empty(N, dtype=torch.uint8, device=dev)
+    graphs = torch.empty(B * N, dtype=torch.uint8, device=dev)
+    for k in range(DISTINCT):
+        depix.graph(d_in[k * N * 4:], W, H, 4 * W, depix.LAYOUT_RGBA, p, fused, stream=stream)
+        depix.resolve_heuristics(fused, W, H, graphs[k * N:], stream=stream)
+    for k in range(DISTINCT, B):
+        graphs[k * N:(k + 1) * N].copy_(graphs[(k % DISTINCT) * N:(k % DISTINCT + 1) * N])
+    max_nodes, max_walks = N, N // 4
+    scratch = torch.empty(B * N, dtype=torch.uint8, device=dev)
+    nodes = torch.empty(B * max_nodes, dtype=torch.int32, device=dev)
+    edges = torch.empty(B * max_nodes, dtype=torch.int8, device=dev)
+    offs = torch.empty(B * (max_walks + 1), dtype=torch.int32, device=dev)
+    counts = torch.empty(3 * B, dtype=torch.int32, device=dev)
+
+    def step():
+        depix.border_walks(graphs, W, H, B, scratch, nodes, edges, offs, max_nodes, max_walks, counts, stream)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    steps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    c = counts.cpu().numpy().reshape(B, 3)
+    assert not c[:, 2].any(), "border-walk capacity ran out"
+    out = {"workload": f"{B} resolved graphs {W}x{H} ({DISTINCT} distinct frames), one warp per frame",
+           "frames_per_s": round(B / (ms / 1e3), 1), "ms_per_batch": round(ms, 3), "steps": steps,
+           "walks_per_frame": round(float(c[:, 0].mean()), 1), "nodes_per_frame": round(float(c[:, 1].mean()), 1)}
+    if cpu:
+        if ORACLE not in sys.path:
+            sys.path.insert(0, ORACLE)
+        import oracle as O
+        g0 = graphs[:N].cpu().numpy()
+        t0 = time.perf_counter()
+        n = 0
+        while n < 8 or time.perf_counter() - t0 < 1.0:
+            O.border_walks(g0, W, H)
+            n += 1
+        out["cpu_baseline"] = {"frames_per_s": round(n / (time.perf_counter() - t0), 1), "cores": 1, "kind": "port",
+                               "sample": f"{n} walks of one frame through the CPU oracle (oracle/depix_oracle.c)"}
+    return out
 
 
 def run_sprites(args, dev, stream):

@@ -137,9 +137,31 @@ depix_status depix_emit_vbo(const uint8_t* d_img, int w, int h, int widthstep, d
 
 /* Connected components of a resolved graph over its set bits: every node
  * gets the minimum linear index of its component. d_labels: w*h int32.
- * (New stage: the reference has only an unbuilt sequential border walk,
- * cc_functions.cu:348-503.) */
+ * (New stage: the reference has only a sequential border walk,
+ * cc_functions.cu:348-503, which depix_border_walks provides.) */
 depix_status depix_label_components(const uint8_t* d_graph, int w, int h, int32_t* d_labels, depix_stream s);
+
+/* Border walks of the components of nframes resolved graphs (frame f at
+ * d_graph + f*w*h), the input of the reference's spline export
+ * (extractBorderPoints, cc_functions.cu:348-503), as its recorded output
+ * alex_png.txt lists them: nodes in scan order start walks unless internal
+ * (byte 90) or already listed; a walk leaves by the node's first link in the
+ * reference's clockwise link order and turns clockwise at every node until
+ * it closes on its start; a walk that enters an internal, listed or
+ * discarded node first is dropped (its last node discarded, its start left
+ * unlisted). A node without links is a walk of its own.
+ *  - d_scratch: w*h*nframes bytes of state, overwritten;
+ *  - walk k of frame f: nodes (linear indices) d_nodes[f*max_nodes +
+ *    d_offsets[f*(max_walks+1) + k] ...] up to offset k+1, and per node the
+ *    link it leaves by in d_edges (int8, -1 for a node without links);
+ *  - d_counts[3*f ..]: walks, nodes, and 1 when max_nodes or max_walks ran
+ *    out (the outputs then hold the walks completed before).
+ * The walks of a frame depend on each other in scan order: one warp per
+ * frame walks them sequentially, so a batch of frames is the efficient
+ * call. */
+depix_status depix_border_walks(const uint8_t* d_graph, int w, int h, int nframes, uint8_t* d_scratch, int32_t* d_nodes,
+                                int8_t* d_edges, int32_t* d_offsets, int max_nodes, int max_walks, int32_t* d_counts,
+                                depix_stream s);
 
 /* Headless raster of a resolved graph (replaces glDrawArrays over the VBO,
  * simpleVBO.cpp:236-285): rebuilds every cell's (optionally subdivided,

@@ -91,6 +91,17 @@ static inline unsigned gat(const uint8_t* g, int w, int h, int i, int j)
     return g[j * w + i];
 }
 
+/* bits of a node whose neighbour lies inside the image */
+static inline unsigned inside_bits(int x, int y, int w, int h)
+{
+    unsigned m = 0xFFu;
+    if (x == 0) m &= ~0x29u;     /* 0, 3, 5 */
+    if (x == w - 1) m &= ~0x94u; /* 2, 4, 7 */
+    if (y == 0) m &= ~0xE0u;     /* 5, 6, 7 */
+    if (y == h - 1) m &= ~0x07u; /* 0, 1, 2 */
+    return m;
+}
+
 /* Trivial crossing removal (crossCheck_4, graph_functions.cu:1211-1274): a
  * node drops a diagonal when the 2x2 block that diagonal crosses is fully
  * 4-connected. Only orthogonal bits are read, so in-place update is exact. */
@@ -830,6 +841,150 @@ void orc_label_cc(const uint8_t* g, int w, int h, int32_t* labels)
             }
     for (int k = 0; k < n; k++) labels[k] = uf_find(p, k);
     free(p);
+}
+
+/* ---------------------------------------------------------- border walks */
+
+/* Link order of the border walk (cc_functions.cu:48-100, 127-183): the
+ * reference enumerates a node's links clockwise from up-left as clock
+ * positions 0..7 and maps them to node bits (getRealLinkIndex) and back
+ * (getClockLinkIndex). */
+static const int REAL_OF_CLOCK[8] = {0, 1, 2, 4, 7, 6, 5, 3};
+static const int CLOCK_OF_REAL[8] = {0, 1, 2, 7, 3, 6, 5, 4};
+
+static int popc8(unsigned v)
+{
+    int c = 0;
+    for (int e = 0; e < 8; e++) c += bit_of(v, e);
+    return c;
+}
+
+/* getFirstLink (cc_functions.cu:107-119) */
+static int first_link(unsigned v)
+{
+    for (int c = 0; c < 8; c++)
+        if (bit_of(v, REAL_OF_CLOCK[c])) return REAL_OF_CLOCK[c];
+    return -1;
+}
+
+/* nextEdgeCounterClockwise (cc_functions.cu:265-287): the link met first
+ * counter-clockwise from e, e itself on a valence-1 node */
+static int next_ccw(unsigned v, int e)
+{
+    if (popc8(v) == 1) return e;
+    int c = CLOCK_OF_REAL[e];
+    for (int k = c + 7; k >= c + 1; k--)
+        if (bit_of(v, REAL_OF_CLOCK[k % 8])) return REAL_OF_CLOCK[k % 8];
+    return e;
+}
+
+/* the link a walk leaves a node of links v by after arriving along e
+ * (nextNodeClockwise, cc_functions.cu:296-318): clockwise from the link back,
+ * the link back itself on a valence-1 node (and, not in the reference, on a
+ * node without links, which only a malformed graph leads to) */
+static int next_cw(unsigned v, int e)
+{
+    int back = 7 - e;
+    if (popc8(v) == 1) return back;
+    int c = CLOCK_OF_REAL[back];
+    for (int k = c + 1; k <= c + 7; k++)
+        if (bit_of(v, REAL_OF_CLOCK[k % 8])) return REAL_OF_CLOCK[k % 8];
+    return back;
+}
+
+/* Border walks of the graph's components in the form the reference's spline
+ * export recorded them (extractBorderPoints, cc_functions.cu:348-503, and
+ * its output alex_png.txt). Nodes are taken in scan order; a node that is
+ * internal (byte 90) or already listed starts no walk. A walk leaves its
+ * start by its first link and turns clockwise at every node until its next
+ * move would enter the start again along the link the start's
+ * counter-clockwise turn gives; it is recorded (every node listed) unless it
+ * enters an internal, listed or discarded node first. A walk that stops
+ * there marks its last recorded node discarded and leaves its start
+ * unlisted: that is how the recorded file was made (all 21 walks of
+ * alex_png.txt follow from it), where the checked-in loop keeps the start
+ * listed and would drop walks 4 and 7 of that file. Not in the reference: a
+ * node without links is a walk of its own (the reference reads past its
+ * link table there), links toward outside the image are ignored, and a walk
+ * longer than 8 w h + 8 steps stops as above.
+ *
+ * Writes walk k's nodes to nodes[offsets[k] .. offsets[k+1]) and the link
+ * each leaves by to edges[] (-1 for a node without links); returns the walk
+ * count, or -1 when max_nodes or max_walks would be exceeded (outputs up to
+ * the last complete walk). *n_nodes gets the nodes written. */
+int orc_border_walks(const uint8_t* g, int w, int h, int32_t* nodes, int8_t* edges, int32_t* offsets, int max_nodes,
+                     int max_walks, int* n_nodes)
+{
+    const int n = w * h;
+    uint8_t* fl = (uint8_t*)calloc((size_t)n + 1, 1); /* bit 0 listed, bit 1 discarded */
+    int nw = 0, pos = 0, trunc = 0;
+    const long long limit = 8LL * n + 8;
+    offsets[0] = 0;
+#define NODE(x, y) (gat(g, w, h, (x), (y)) & inside_bits((x), (y), w, h))
+    for (int y = 0; y < h && !trunc; y++)
+        for (int x = 0; x < w; x++) {
+            const int p = y * w + x;
+            const unsigned v0 = NODE(x, y);
+            if (v0 == 90 || (fl[p] & 1)) continue;
+            if (v0 == 0) {
+                if (nw >= max_walks || pos >= max_nodes) {
+                    trunc = 1;
+                    break;
+                }
+                nodes[pos] = p;
+                edges[pos++] = -1;
+                fl[p] |= 1;
+                offsets[++nw] = pos;
+                continue;
+            }
+            fl[p] |= 1;
+            int e = first_link(v0);
+            const int arr = next_ccw(v0, e);
+            const int start = pos;
+            int over = 0, last = p; // over: a node did not fit (the walk is then not recorded)
+            if (pos < max_nodes) {
+                nodes[pos] = p;
+                edges[pos++] = (int8_t)e;
+            } else {
+                over = 1;
+            }
+            int cx = x, cy = y, ok = 1;
+            long long steps = 0;
+            while (!(cx + DI[e] == x && cy + DJ[e] == y && 7 - e == arr)) {
+                cx += DI[e];
+                cy += DJ[e];
+                const int cp = cy * w + cx;
+                const unsigned v = NODE(cx, cy);
+                e = next_cw(v, e);
+                if (v == 90 || fl[cp] || ++steps > limit) {
+                    fl[last] |= 2;
+                    fl[p] &= (uint8_t)~1u;
+                    pos = start;
+                    ok = 0;
+                    break;
+                }
+                last = cp;
+                if (pos < max_nodes) {
+                    nodes[pos] = cp;
+                    edges[pos++] = (int8_t)e;
+                } else {
+                    over = 1;
+                }
+            }
+            if (ok) {
+                if (over || nw >= max_walks) {
+                    pos = start;
+                    trunc = 1;
+                    break;
+                }
+                for (int q = start; q < pos; q++) fl[nodes[q]] |= 1;
+                offsets[++nw] = pos;
+            }
+        }
+#undef NODE
+    free(fl);
+    *n_nodes = pos;
+    return trunc ? -1 : nw;
 }
 
 /* ------------------------------------------------------------ whole frame */

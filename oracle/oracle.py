@@ -51,6 +51,9 @@ def lib():
         L.orc_hull_table.argtypes = [_i32p, _i8p]
         L.orc_raster.argtypes = [_f32p, _u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_label_cc.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _i32p]
+        L.orc_border_walks.restype = ctypes.c_int
+        L.orc_border_walks.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _i32p, _i8p, _i32p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         vp = ctypes.c_void_p
         L.orc_frame.restype = ctypes.c_int
         L.orc_frame.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -134,6 +137,23 @@ def label_cc(graph_resolved, w, h):
     out = np.zeros(w * h, np.int32)
     lib().orc_label_cc(np.ascontiguousarray(graph_resolved, np.uint8), w, h, out)
     return out
+
+
+def border_walks(graph, w, h, max_nodes=None, max_walks=None):
+    """Border walks of a resolved graph: a list of (nodes, edges) per walk, or
+    None when the capacities run out."""
+    n = w * h
+    max_nodes = 8 * n + 8 if max_nodes is None else max_nodes
+    max_walks = n if max_walks is None else max_walks
+    nodes = np.zeros(max(max_nodes, 1), np.int32)
+    edges = np.zeros(max(max_nodes, 1), np.int8)
+    offs = np.zeros(max_walks + 1, np.int32)
+    used = ctypes.c_int(0)
+    k = lib().orc_border_walks(np.ascontiguousarray(graph, np.uint8).reshape(-1), w, h, nodes, edges, offs,
+                               max_nodes, max_walks, ctypes.byref(used))
+    if k < 0:
+        return None
+    return [(nodes[offs[i]:offs[i + 1]].tolist(), edges[offs[i]:offs[i + 1]].tolist()) for i in range(k)]
 
 
 # ----------------------------------------------------------- reference build

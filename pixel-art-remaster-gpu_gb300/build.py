@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdepix.so")
-UNITS = ["depix_graph.cu", "depix_geom.cu", "depix_api.cu", "depix_queue.cu", "depix_refine.cu", "depix_static.cu"]
+UNITS = ["depix_graph.cu", "depix_geom.cu", "depix_api.cu", "depix_queue.cu", "depix_refine.cu", "depix_static.cu",
+         "depix_walks.cu"]
 HEADERS = ["depix_device.cuh", "depix_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",

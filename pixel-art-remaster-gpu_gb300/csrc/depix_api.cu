@@ -310,6 +310,19 @@ depix_status depix_label_components(const uint8_t* d_graph, int w, int h, int32_
     return DEPIX_OK;
 }
 
+depix_status depix_border_walks(const uint8_t* d_graph, int w, int h, int nframes, uint8_t* d_scratch, int32_t* d_nodes,
+                                int8_t* d_edges, int32_t* d_offsets, int max_nodes, int max_walks, int32_t* d_counts,
+                                depix_stream s)
+{
+    DEPIX_TRY(check_size(w, h));
+    if (nframes < 1) return arg_fail("nframes must be >= 1");
+    if (max_nodes < 1 || max_walks < 1) return arg_fail("capacities must be >= 1");
+    if (!d_graph || !d_scratch || !d_nodes || !d_edges || !d_offsets || !d_counts) return arg_fail("NULL pointer");
+    DEPIX_CK(launch_border_walks(d_graph, w, h, nframes, d_scratch, d_nodes, d_edges, d_offsets, max_nodes, max_walks,
+                                 d_counts, S(s)));
+    return DEPIX_OK;
+}
+
 depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, depix_stream s)
 {
     if (n && (!d_px3 || !d_words)) return arg_fail("NULL pointer");

@@ -164,6 +164,9 @@ void set_last_error(const std::string& msg);
 // graph stage
 cudaError_t launch_graph(const FrameBatch& b, int nframes, uint32_t thr, bool fuse_trivial, cudaStream_t s);
 cudaError_t launch_trivial(uint8_t* g, int w, int h, cudaStream_t s);
+cudaError_t launch_border_walks(const uint8_t* graph, int w, int h, int nframes, uint8_t* flags, int32_t* nodes,
+                                int8_t* edges, int32_t* offsets, int max_nodes, int max_walks, int32_t* counts,
+                                cudaStream_t s);
 cudaError_t launch_heuristics(const GraphBatch& b, int nframes, cudaStream_t s);
 // heuristics with each tile's local component labels fused in, then the
 // label stage's remainder (merge across the 64x16 tile borders, flatten)

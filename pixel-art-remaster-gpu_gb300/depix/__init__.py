@@ -78,6 +78,7 @@ def lib():
         _sig(L, "depix_triangulate", [_vp, _vp, _i, _i, _vp])
         _sig(L, "depix_emit_vbo", [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp])
         _sig(L, "depix_label_components", [_vp, _i, _i, _vp, _vp])
+        _sig(L, "depix_border_walks", [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp])
         _sig(L, "depix_raster", [_vp, _i, _i, _i, _i, _vp, P, _vp, _vp])
         _sig(L, "depix_context_create", [ctypes.POINTER(_vp), ctypes.c_size_t, _i])
         _sig(L, "depix_context_destroy", [_vp])
@@ -181,6 +182,43 @@ def emit_vbo(img, w, h, ws, layout, diagram, ec, pos, col, stream=None):
 
 def label_components(g, w, h, labels, stream=None):
     _check(lib().depix_label_components(ptr(g), w, h, ptr(labels), stream_ptr(stream)), "depix_label_components")
+
+
+def border_walks(g, w, h, nframes, scratch, nodes, edges, offsets, max_nodes, max_walks, counts, stream=None):
+    _check(lib().depix_border_walks(ptr(g), w, h, nframes, ptr(scratch), ptr(nodes), ptr(edges), ptr(offsets),
+                                    max_nodes, max_walks, ptr(counts), stream_ptr(stream)), "depix_border_walks")
+
+
+def border_walk_lists(g, w, h, nframes=1, max_nodes=None, max_walks=None, stream=None):
+    """Border walks of nframes resolved graphs on the device (a torch uint8
+    tensor, frames w*h bytes apart): per frame, a list of (nodes, edges)
+    walks and whether a capacity ran out."""
+    import torch
+    n = w * h
+    max_nodes = 4 * n + 16 if max_nodes is None else max_nodes
+    max_walks = n if max_walks is None else max_walks
+    dev = g.device
+    scratch = torch.empty(n * nframes, dtype=torch.uint8, device=dev)
+    nodes = torch.empty(max_nodes * nframes, dtype=torch.int32, device=dev)
+    edges = torch.empty(max_nodes * nframes, dtype=torch.int8, device=dev)
+    offsets = torch.empty((max_walks + 1) * nframes, dtype=torch.int32, device=dev)
+    counts = torch.empty(3 * nframes, dtype=torch.int32, device=dev)
+    border_walks(g, w, h, nframes, scratch, nodes, edges, offsets, max_nodes, max_walks, counts, stream)
+    c = counts.cpu().numpy().reshape(nframes, 3)
+    nd, ed, of = nodes.cpu().numpy(), edges.cpu().numpy(), offsets.cpu().numpy()
+    out = []
+    for f in range(nframes):
+        o = of[f * (max_walks + 1):f * (max_walks + 1) + c[f, 0] + 1]
+        base = f * max_nodes
+        out.append(([(nd[base + o[k]:base + o[k + 1]].tolist(), ed[base + o[k]:base + o[k + 1]].tolist())
+                     for k in range(c[f, 0])], bool(c[f, 2])))
+    return out
+
+
+def format_walks(walks) -> str:
+    """Walks as the reference's spline export wrote them (alex_png.txt):
+    one line 'Spline: k - ' with ' node, ' per node."""
+    return "".join(f"Spline: {k} - " + "".join(f" {v}, " for v in nodes) + "\n" for k, (nodes, _) in enumerate(walks))
 
 
 def raster(img, w, h, ws, layout, g, p, out, stream=None):

@@ -16,11 +16,13 @@ stage bodies (oracle/_ref). Writes, next to this script:
                       (kernel.cu:291-293, an 8x8 image; kernel.cu:296, a 24x24
                       image) and the reference's cells/triangles for them;
 * ``borders.json`` -- the per-component border walks of the 24x24 image
-                      (alex_png.txt:1-21);
+                      (alex_png.txt:1-21) and the chain code recorded for
+                      its walk from node 5 (alex_png.txt:25-44);
 * ``yuv.json``     -- SHA-256 of the reference's packed YUV word for all 2^24
                       colours (graph_functions.cu:80-131) plus a sample.
 
 usage: python tests/golden/make_golden.py [REFERENCE_DIR]
+       python tests/golden/make_golden.py --borders [REFERENCE_DIR]   (borders.json only)
 """
 from __future__ import annotations
 
@@ -111,6 +113,23 @@ def parse_dump(src, label, size):
     return np.array(vals, np.int64).astype(np.uint8)
 
 
+def write_borders(ref_dir):
+    """borders.json from alex_png.txt: the walks ("Spline: k - ..." lines)
+    and the chain code the file records for the walk from node 5 ("index: i,
+    edge: e" lines)."""
+    walks, chain = {}, {"nodes": [], "edges": []}
+    for line in open(os.path.join(ref_dir, "alex_png.txt")):
+        m = re.match(r"Spline: (\d+) -(.*)", line)
+        if m:
+            walks[int(m.group(1))] = [int(t) for t in re.findall(r"\d+", m.group(2))]
+        m = re.match(r"index: (\d+), edge: (\d+)", line)
+        if m:
+            chain["nodes"].append(int(m.group(1)))
+            chain["edges"].append(int(m.group(2)))
+    with open(os.path.join(HERE, "borders.json"), "w") as fh:
+        json.dump({"image": "alex", "size": [24, 24], "walks": walks, "chain_from_5": chain}, fh, indent=0)
+
+
 def main(ref_dir="/root/reference"):
     for tr in (5, 48):
         if not O.ref_available(tr):
@@ -154,13 +173,7 @@ def main(ref_dir="/root/reference"):
         dz[f"{name}/pos"] = defined_pos(f.pos, f.ec)
     np.savez_compressed(os.path.join(HERE, "dumps.npz"), **dz)
 
-    walks = {}
-    for line in open(os.path.join(ref_dir, "alex_png.txt")):
-        m = re.match(r"Spline: (\d+) -(.*)", line)
-        if m:
-            walks[int(m.group(1))] = [int(t) for t in re.findall(r"\d+", m.group(2))]
-    with open(os.path.join(HERE, "borders.json"), "w") as fh:
-        json.dump({"image": "alex", "size": [24, 24], "walks": walks}, fh, indent=0)
+    write_borders(ref_dir)
 
     allc = np.stack(np.meshgrid(np.arange(256), np.arange(256), np.arange(256), indexing="ij"), -1)
     allc = allc.reshape(-1, 3).astype(np.uint8)
@@ -174,4 +187,7 @@ def main(ref_dir="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if sys.argv[1:2] == ["--borders"]:
+        write_borders(*(sys.argv[2:] or ["/root/reference"]))
+    else:
+        main(*sys.argv[1:])
