@@ -1380,15 +1380,21 @@ int queue_raster_blocks_per_sm(const QueueBatch& q) { DEPIX_RQ_DISPATCH(raster_q
 
 // 32x32-cell tiles up to scale 4 (more subdivided cells per block to share
 // the work), 32x16 above (the footprint masks grow with the scale)
+// A single frame fills a fraction of the SMs, so it takes tiles half as high
+// at x4 (twice the blocks, each half as long); batches keep the 32-row tiles.
 cudaError_t launch_mask_raster(const RasterBatch& b, int nframes, const uint32_t* lut, cudaStream_t s)
 {
     if (b.layout == DEPIX_LAYOUT_RGBA) {
-        if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4, 32>(b, nframes, lut, s);
+        if (b.scale == 4)
+            return nframes == 1 ? launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4, 16>(b, nframes, lut, s)
+                                : launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 4, 32>(b, nframes, lut, s);
         if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 8, 16>(b, nframes, lut, s);
         if (b.scale < 4) return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0, 32>(b, nframes, lut, s);
         return launch_mask_raster_t<DEPIX_LAYOUT_RGBA, 0, 16>(b, nframes, lut, s);
     }
-    if (b.scale == 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4, 32>(b, nframes, lut, s);
+    if (b.scale == 4)
+        return nframes == 1 ? launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4, 16>(b, nframes, lut, s)
+                            : launch_mask_raster_t<DEPIX_LAYOUT_BGR, 4, 32>(b, nframes, lut, s);
     if (b.scale == 8) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 8, 16>(b, nframes, lut, s);
     if (b.scale < 4) return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 32>(b, nframes, lut, s);
     return launch_mask_raster_t<DEPIX_LAYOUT_BGR, 0, 16>(b, nframes, lut, s);
