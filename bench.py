@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--no-stream", action="store_true")
     ap.add_argument("--no-vote", action="store_true")
     ap.add_argument("--no-walks", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--large-frames", type=int, default=16, help="640x480 frames per step in the x8 leg")
+    ap.add_argument("--large-only", action="store_true", help="run only the 640x480 x8 leg (for profiling)")
     ap.add_argument("--stream-frames", type=int, default=512)
     return ap.parse_args()
 
@@ -312,6 +315,7 @@ def run_ours(args, rank, world, local_rank):
                 "steps": vsteps, "stage_ms_per_step": {k: round(v[0] / max(v[2], 1), 4) for k, v in vst.items()}}
 
     walks = None if args.no_walks else run_walks(args, dev, stream, d_in, cpu=(rank == 0 and world == 1 and not args.no_cpu))
+    large = None if args.no_large else run_large(args, dev, stream)
 
     sprites = None if args.no_sprites else run_sprites(args, dev, stream)
     refine = None if args.no_refine else run_refine(args, dev, stream, cpu=(rank == 0 and world == 1 and not args.no_cpu))
@@ -333,8 +337,57 @@ def run_ours(args, rank, world, local_rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
                 "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
-                "refine": refine, "stream": stream_leg, "vote": vote, "border_walks": walks}
+                "refine": refine, "stream": stream_leg, "vote": vote, "border_walks": walks,
+                "large_x8": large}
         print(json.dumps(line))
+
+
+def run_large(args, dev, stream):
+    """The 640x480 workload upscaled x8 (5120x3840 per frame), batched with
+    labels: frames/s, per-stage times and the raster's roofline."""
+    import numpy as np
+    import torch
+    import depix
+    from depix import synth
+    B, LW, LH, LS = args.large_frames, 640, 480, 8
+    imgs = np.stack([synth.frame_large(s) for s in range(B)])
+    in_bytes, out_px = LW * LH * 4, LW * LH * LS * LS
+    d_img = torch.from_numpy(imgs.reshape(-1)).to(dev)
+    d_out = torch.empty(B * out_px * 4, dtype=torch.uint8, device=dev)
+    d_lab = torch.empty(B * LW * LH, dtype=torch.int32, device=dev)
+    ctx = depix.Context(LW * LH, B)
+    p = depix.params(48, 7, 6, True, LS)
+    ws, hs = np.full(B, LW, np.int32), np.full(B, LH, np.int32)
+    in_off = np.arange(B, dtype=np.uint64) * np.uint64(in_bytes)
+    out_off = np.arange(B, dtype=np.uint64) * np.uint64(out_px * 4)
+
+    def step():
+        ctx.batch(ws, hs, in_off, out_off, d_img, p, d_out, d_lab, stream=stream)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 20))
+    ctx.stage_times()
+    ctx.set_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.set_timing(False)
+    ms = e0.elapsed_time(e1) / steps
+    st = {k: round(v[0] / max(v[2], 1), 4) for k, v in ctx.stage_times().items()}
+    ctx.close()
+    alg = B * (LW * LH * (4 + 1) + out_px * 4)
+    peak, peak_kind = measured_peak()
+    achieved = alg / (st["raster"] / 1e3) / 1e9
+    return {"workload": f"{B} frames 640x480 RGBA8 (64 colours, 200 shapes, 10% dither, 2% noise) -> x8 5120x3840, "
+                        "labels, subdivision", "frames_per_s": round(B / (ms / 1e3), 1), "ms_per_step": round(ms, 3),
+            "out_mpix_per_s": round(B * out_px / (ms / 1e3) / 1e6, 1), "steps": steps, "stage_ms_per_step": st,
+            "raster_roofline": {"achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                                "frac": round(achieved / peak, 4), "alg_bytes_per_step": alg}}
 
 
 def run_walks(args, dev, stream, d_in, cpu):
@@ -738,6 +791,14 @@ def main():
         depix_build.build()
     if world > 1:
         torch.distributed.barrier()
+    if args.large_only:
+        import torch
+        torch.cuda.set_device(local_rank)
+        import depix
+        depix.init_device()
+        print(json.dumps({"large_x8": run_large(args, torch.device("cuda", local_rank),
+                                                torch.cuda.current_stream())}))
+        return
     run_ours(args, rank, world, local_rank)
     if world > 1:
         torch.distributed.destroy_process_group()
