@@ -327,9 +327,11 @@ def run_ours(args, rank, world, local_rank):
         n = args.cpu_sample or 4 * cores
         cpu_run(frames, min(cores, n), cores)  # warm
         v = cpu_run(frames, n, cores)
+        v1 = cpu_run(frames, 4, 1)
         cpu = {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} frames of the same workload through the CPU oracle (oracle/depix_oracle.c: graph, "
-                         f"resolution, cells, subdivision, ear clip, VBO fill, labels, x4 raster), {cores} threads"}
+                         f"resolution, cells, subdivision, ear clip, VBO fill, labels, x4 raster), {cores} threads",
+               "single_thread_value": round(v1, 2)}
     ctx.close()
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
