@@ -618,13 +618,46 @@ __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t fr
     cc_merge_border(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, t / kLBorder, t % kLBorder);
 }
 
+// Four consecutive pixels per thread, their labels in one 16-byte load where
+// aligned and their four finds interleaved, so that each thread keeps four
+// independent loads in flight (one find per pixel is bound by load latency).
 __global__ void k_cc_flatten(int32_t* L, int n, size_t frame_stride)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (k >= n) return;
     L += frame_stride * blockIdx.z;
-    const int r = uf_find(L, k);
-    if (L[k] != r) L[k] = r;
+    int32_t* q = L + k;
+    int p[4], x[4];
+    if (k + 3 < n && (reinterpret_cast<uintptr_t>(q) & 15) == 0) {
+        const int4 v = *reinterpret_cast<const int4*>(q);
+        p[0] = v.x;
+        p[1] = v.y;
+        p[2] = v.z;
+        p[3] = v.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; i++) p[i] = k + i < n ? q[i] : k + i;
+    }
+    int first[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        x[i] = k + i;
+        first[i] = p[i];
+    }
+    for (;;) {
+        bool more = false;
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            if (p[i] != x[i]) {
+                x[i] = p[i];
+                p[i] = L[x[i]];
+                more = true;
+            }
+        if (!more) break;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (k + i < n && first[i] != x[i]) q[i] = x[i];
 }
 
 // ------------------------------------------------ uneven batches (queue)
@@ -819,7 +852,7 @@ cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, in
     const int borders = tiles * kHBorder;
     k_cc_merge_h<<<dim3((borders + 127) / 128, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
     const int n = w * h;
-    k_cc_flatten<<<dim3((n + 255) / 256, 1, nframes), 256, 0, s>>>(labels, n, frame_stride);
+    k_cc_flatten<<<dim3((n + 1023) / 1024, 1, nframes), 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }
 
@@ -831,7 +864,7 @@ cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int n
     k_cc_local<<<tiles, 256, 0, s>>>(g, labels, w, h, frame_stride);
     const int borders = tiles.x * tiles.y * kLBorder;
     k_cc_merge<<<dim3((borders + 127) / 128, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
-    dim3 grid((n + 255) / 256, 1, nframes);
+    dim3 grid((n + 1023) / 1024, 1, nframes);
     k_cc_flatten<<<grid, 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }
