@@ -904,7 +904,7 @@ depix_status compat_run(void* pos, void* colorPos, char* img_data, int w, int h,
 {
     DEPIX_TRY(check_size(w, h));
     if (!img_data || ws < 3 * w) return arg_fail("bad host image");
-    depix_params ref{5, 7, 6, 0, 1};
+    depix_params ref{5, 7, 6, 0, 1, 0};
     if (!p) p = &ref;
     DEPIX_TRY(check_params(p));
     DEPIX_TRY(ensure_tables(nullptr));
