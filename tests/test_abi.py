@@ -68,6 +68,12 @@ def test_bad_arguments_are_rejected_before_cuda(L):
     assert b"capacity" in L.depix_last_error()
     # launch shape of a missing context
     assert L.depix_context_set_launch_shape(None, 1, 32, 32) == 1
+    # border walks: no frames, no capacity, a NULL buffer
+    v = ctypes.c_void_p(16)
+    assert L.depix_border_walks(v, 8, 8, 0, v, v, v, v, 16, 16, v, None) == 1
+    assert L.depix_border_walks(v, 8, 8, 1, v, v, v, v, 0, 16, v, None) == 1
+    assert L.depix_border_walks(v, 8, 8, 1, v, v, v, None, 16, 16, v, None) == 1
+    assert L.depix_border_walks(v, 0, 8, 1, v, v, v, v, 16, 16, v, None) == 1
 
 
 def test_default_params(L):
