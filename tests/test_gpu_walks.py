@@ -85,3 +85,21 @@ def test_capacities(cuda):
         assert trunc and len(walks) < len(full)
         assert walks == [(list(a), list(b)) for a, b in full[:len(walks)]]
         assert sum(len(n) for n, _ in walks) <= max_nodes and len(walks) <= max_walks
+
+
+@pytest.mark.parametrize("kind", ["symmetric", "bytes"])
+def test_random_graphs_equal_oracle(cuda, kind):
+    """Random graphs in one batch: symmetric ones like the pipeline's, and
+    arbitrary bytes (links outside the image, asymmetric links, walks that
+    never close)."""
+    import depix
+    from test_walks_random import _symmetric
+    rng = np.random.default_rng(7 if kind == "symmetric" else 8)
+    w, h, n = 23, 17, 6
+    gs = [(_symmetric(rng, w, h, 0.6) if kind == "symmetric" else rng.integers(0, 256, w * h).astype(np.uint8))
+          for _ in range(n)]
+    d = cuda.from_numpy(np.concatenate(gs)).cuda()
+    res = depix.border_walk_lists(d, w, h, nframes=n, max_nodes=8 * w * h + 8, max_walks=w * h)
+    for g, (walks, trunc) in zip(gs, res):
+        assert not trunc
+        assert walks == [(list(a), list(b)) for a, b in O.border_walks(g, w, h)]
