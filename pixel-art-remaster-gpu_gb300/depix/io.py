@@ -210,18 +210,27 @@ def save_raster(path, raster: np.ndarray) -> bytes:
     return write_png(path, np.ascontiguousarray(np.asarray(raster)[::-1]))
 
 
-def read_raw_frames(path, w: int, h: int, layout: str = "rgba", top_down: bool = True):
+def read_raw_frames(path, w: int, h: int, layout: str = "rgba", top_down: bool = True, widthstep: int = 0,
+                    skip: int = 0):
     """Frames of a headerless stream of w x h images (``rgba``: 4 bytes per
-    pixel; ``bgr``: 3, rows packed), yielded as RGBA8 with row 0 at the bottom
-    (flipped when the stream stores the top row first)."""
+    pixel; ``bgr``: 3), yielded as RGBA8 with row 0 at the bottom (flipped
+    when the stream stores the top row first). Rows are ``widthstep`` bytes
+    apart (0: packed); the reference's raw video held its image loader's BGR
+    rows with their 4-byte-aligned stride and was read from frame 40 on
+    (main.cpp:67-75): ``layout="bgr", widthstep=(3 * w + 3) & ~3, skip=40``.
+    ``skip`` frames are passed over first."""
     bpp = {"rgba": 4, "bgr": 3}[layout]
-    size = w * h * bpp
+    stride = widthstep or w * bpp
+    if stride < w * bpp:
+        raise ValueError("widthstep smaller than a row")
+    size = stride * h
     with open(path, "rb") as fh:
+        fh.seek(size * skip)
         while True:
             buf = fh.read(size)
             if len(buf) < size:
                 return
-            px = np.frombuffer(buf, np.uint8).reshape(h, w, bpp)
+            px = np.frombuffer(buf, np.uint8).reshape(h, stride)[:, :w * bpp].reshape(h, w, bpp)
             if layout == "bgr":
                 img = np.empty((h, w, 4), np.uint8)
                 img[..., 0], img[..., 1], img[..., 2], img[..., 3] = px[..., 2], px[..., 1], px[..., 0], 255

@@ -256,3 +256,17 @@ def test_host_batch_in_chunks_equals_the_device_batch(cuda, kind):
     assert torch.equal(h_out, d_out.cpu())
     assert torch.equal(h_lab, d_lab.cpu())
     ctx.close()
+
+
+def test_stream_front_end(cuda):
+    """depix.stream.upscale_stream with its own context: uneven frames in
+    batches of 4 through depix_batch_host, rasters and labels in order."""
+    import depix
+    from depix import stream
+    imgs = synth.sprites(9, seed=41)
+    out = list(stream.upscale_stream(imgs, depix.params(), batch=4, labels=True))
+    assert len(out) == len(imgs)
+    for img, (raster, lab) in zip(imgs, out):
+        r, l = _oracle(img, 4)
+        assert_raster_close(raster, r)
+        assert np.array_equal(lab, l)
