@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=1024, help="frames per step")
     ap.add_argument("--plain-frames", type=int, default=300)
-    ap.add_argument("--e2e-steps", type=int, default=0, help="default: max(3, steps // 20)")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="default: max(20, steps // 5)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU-baseline sample (default 4 x cores)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sprites", type=int, default=4096, help="sprites in the uneven-batch leg")
@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--large-frames", type=int, default=16, help="640x480 frames per step in the x8 leg")
     ap.add_argument("--large-only", action="store_true", help="run only the 640x480 x8 leg (for profiling)")
     ap.add_argument("--stream-frames", type=int, default=512)
+    ap.add_argument("--latency-frames", type=int, default=400, help="plain calls in the latency sweep")
     return ap.parse_args()
 
 
@@ -84,31 +85,56 @@ def make_frames(n_distinct):
 # ------------------------------------------------------------- CPU baseline
 
 
-def cpu_path_frame(img):
-    """The whole path on one frame through the CPU oracle."""
+def cpu_path_frame(img, kind):
+    """The whole path on one frame on the CPU. kind "reference": the
+    reference's own per-pixel stage bodies (its host build, oracle/_ref) from
+    the graph to the VBO, then the component labels and the x4 raster of that
+    VBO through the CPU oracle (the reference draws with OpenGL, unavailable
+    here, and has no labelling stage). kind "port": all of it through the CPU
+    oracle (oracle/depix_oracle.c, a C restatement of the same stages)."""
     import oracle as O
     from depix import synth
     bgr, ws = synth.rgba_to_bgr(img)
-    f = O.frame(bgr, W, H, ws, 1, (48, 7, 6))
-    O.label_cc(f.graph, W, H)
-    O.raster(f.pos, f.col, W, H, SCALE)
+    if kind == "reference":
+        graph, pos, col = O.ref_frame_vbo(bgr, W, H, ws, 1, 48)
+    else:
+        f = O.frame(bgr, W, H, ws, 1, (48, 7, 6))
+        graph, pos, col = f.graph, f.pos, f.col
+    O.label_cc(graph, W, H)
+    O.raster(pos, col, W, H, SCALE)
 
 
-def cpu_run(frames, n_frames, threads):
-    """frames/s of the CPU oracle over n_frames frames on `threads` threads
+def cpu_run(frames, n_frames, threads, kind):
+    """frames/s of the CPU path over n_frames frames on `threads` threads
     (the C calls release the GIL)."""
     from concurrent.futures import ThreadPoolExecutor
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        list(ex.map(lambda k: cpu_path_frame(frames[k % len(frames)]), range(n_frames)))
+        list(ex.map(lambda k: cpu_path_frame(frames[k % len(frames)], kind), range(n_frames)))
     return n_frames / (time.perf_counter() - t0)
 
 
 def cpu_setup():
-    sys.path.insert(0, ORACLE)
+    """Builds the CPU oracle and the reference's host build (from the staged
+    reference sources, for this machine's CPU); returns the core count and
+    the kind of CPU path available ("reference" when the host build is)."""
+    if ORACLE not in sys.path:
+        sys.path.insert(0, ORACLE)
     import oracle as O
     O.build()
-    return os.cpu_count() or 1
+    kind = "reference" if O.build_ref(gpu=False) else "port"
+    return os.cpu_count() or 1, kind
+
+
+CPU_SAMPLE = {
+    "reference": "the reference's own per-pixel stage bodies (graph_functions.cu, diagram_functions.cu, "
+                 "subdivision_functions.cu, triangulate_functions.cu, point.cu; host build with g++ -O2, Y 48, "
+                 "oracle/ref_driver.cpp replaying launch_kernel's stage order) from the graph to the VBO, then "
+                 "labels and the x4 raster of that VBO through the CPU oracle (the reference's raster is an OpenGL "
+                 "draw, unavailable here; it has no labelling stage)",
+    "port": "the CPU oracle (oracle/depix_oracle.c, a C restatement of the reference's stage bodies: graph, "
+            "resolution, cells, subdivision, ear clip, VBO fill, labels, x4 raster)",
+}
 
 
 # ------------------------------------------------------------------- clocks
@@ -253,7 +279,7 @@ def run_ours(args, rank, world, local_rank):
 
     # end to end through the host-buffer call, copies inside the timed region
     e2e = None
-    e2e_steps = args.e2e_steps or max(3, args.steps // 20)
+    e2e_steps = args.e2e_steps or max(20, args.steps // 5)
     h_in = torch.from_numpy(tiled.reshape(-1)).pin_memory()
     h_out = torch.empty(B * out_px * 4, dtype=torch.uint8).pin_memory()
     h_lab = torch.empty(B * W * H, dtype=torch.int32).pin_memory()
@@ -266,32 +292,18 @@ def run_ours(args, rank, world, local_rank):
     e2e_s = time.perf_counter() - t0
     e2e_v = replicas.job_throughput(B * e2e_steps, e2e_s, dev)
     e2e = {"value": round(e2e_v, 1), "unit": UNIT, "h2d_bytes_per_step": B * in_bytes,
-           "d2h_bytes_per_step": B * (out_px * 4 + W * H * 4), "steps": e2e_steps}
-    # spot check of the e2e output against the device path
-    assert torch.equal(h_out[: out_px * 4], d_out[: out_px * 4].cpu()), "e2e output differs from device path"
+           "d2h_bytes_per_step": B * (out_px * 4 + W * H * 4), "steps": e2e_steps,
+           "timed_s": round(e2e_s, 3)}
 
-    # plain per-frame path: one launch per stage and frame
-    pf = max(args.plain_frames, 10)
-    ctx1 = depix.Context(W * H, 1)
-    lat = []
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(pf)]
-    for k in range(5):
-        ctx1.frame(d_in[k * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out, None, d_lab, stream=stream)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(pf):
-        a, b = evs[k]
-        a.record(stream)
-        f = k % B
-        ctx1.frame(d_in[f * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out[f * out_px * 4:], None,
-                   d_lab[f * W * H:], stream=stream)
-        b.record(stream)
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
-    lat = sorted(a.elapsed_time(b) for a, b in evs)
-    plain = {"frames_per_s": round(pf / plain_s, 1), "p50_ms_per_frame": round(lat[len(lat) // 2], 4),
-             "p99_ms_per_frame": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4), "frames": pf}
-    ctx1.close()
+    # frames of both paths against the CPU oracle (a C restatement of the
+    # reference's stage bodies): rasters and labels of a few frames of the
+    # last device-resident batch and of the last host-buffer batch
+    check = check_against_oracle(frames, d_out, d_lab, h_out, h_lab, B)
+
+    # per-frame latency, plain and batched: from the start of a frame's (or
+    # batch's) upload from pinned host memory to its last kernel, on the
+    # stream, over back-to-back calls; frames/s over the same calls
+    latency = run_latency(args, dev, stream, ctx, frames, B)
 
     # the same batch with the weighted-vote heuristics (depix_params.vote)
     vote = None
@@ -323,25 +335,133 @@ def run_ours(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cores = cpu_setup()
+        cores, kind = cpu_setup()
         n = args.cpu_sample or 4 * cores
-        cpu_run(frames, min(cores, n), cores)  # warm
-        v = cpu_run(frames, n, cores)
-        v1 = cpu_run(frames, 4, 1)
-        cpu = {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} frames of the same workload through the CPU oracle (oracle/depix_oracle.c: graph, "
-                         f"resolution, cells, subdivision, ear clip, VBO fill, labels, x4 raster), {cores} threads",
+        cpu_run(frames, min(cores, n), cores, kind)  # warm
+        v = cpu_run(frames, n, cores, kind)
+        v1 = cpu_run(frames, 4, 1, kind)
+        cpu = {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": f"{n} frames of the same workload, {cores} threads, one frame each: " + CPU_SAMPLE[kind],
                "single_thread_value": round(v1, 2)}
+        if kind == "reference":
+            cpu["port_value"] = round(cpu_run(frames, n, cores, "port"), 2)
     ctx.close()
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)",
-                "config": workload_config(B), "e2e": e2e, "plain": plain, "roofline": roofline,
+                "config": workload_config(B), "e2e": e2e, "plain": plain, "latency": latency,
+                "oracle_check": check, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "sprites": sprites,
                 "refine": refine, "stream": stream_leg, "vote": vote, "border_walks": walks,
                 "large_x8": large}
         print(json.dumps(line))
+
+
+def check_against_oracle(frames, d_out, d_lab, h_out, h_lab, B):
+    """Frames 0, 1 and B-1 of the device-resident batch (d_out, d_lab) and of
+    the host-buffer batch (h_out, h_lab) against the CPU oracle: raster and
+    labels bit-exact. Raises on a mismatch."""
+    import numpy as np
+    if ORACLE not in sys.path:
+        sys.path.insert(0, ORACLE)
+    import oracle as O
+    from depix import synth
+    O.build()
+    out_px = W * H * SCALE * SCALE
+    checked = []
+    for k in sorted({0, 1, B - 1}):
+        img = frames[k % len(frames)]
+        bgr, ws = synth.rgba_to_bgr(img)
+        f = O.frame(bgr, W, H, ws, 1, (48, 7, 6))
+        want_r = O.raster(f.pos, f.col, W, H, SCALE).reshape(-1)
+        want_l = O.label_cc(f.graph, W, H)
+        for name, r, l in (("device", d_out, d_lab), ("host", h_out, h_lab)):
+            got_r = r[k * out_px * 4:(k + 1) * out_px * 4].cpu().numpy()
+            got_l = l[k * W * H:(k + 1) * W * H].cpu().numpy()
+            assert np.array_equal(got_r, want_r), f"{name} batch frame {k}: raster differs from the oracle"
+            assert np.array_equal(got_l, want_l), f"{name} batch frame {k}: labels differ from the oracle"
+        checked.append(k)
+    return {"frames": checked, "paths": ["device batch", "host-buffer batch"],
+            "compared": "x4 raster and component labels, bit-exact, against the CPU oracle"}
+
+
+def run_latency(args, dev, stream, ctx, frames, B_max):
+    """Per-frame latency of the plain path (one depix_frame call per frame)
+    and of batches of 8, 32, 128 and 1024 frames through depix_batch, each
+    call preceded by the upload of its frames from pinned host memory. A
+    frame's latency is its call's: from the start of the upload to the end
+    of the call's last kernel (CUDA events on the stream). frames/s: frames
+    over the wall time of the back-to-back calls."""
+    import numpy as np
+    import torch
+    import depix
+    in_bytes, out_px = W * H * 4, W * H * SCALE * SCALE
+    p = depix.params(48, 7, 6, True, SCALE)
+    n_frames = max(args.latency_frames, 64)
+    h_all = torch.from_numpy(np.ascontiguousarray(np.resize(frames, (max(B_max, 1024), H, W, 4))).reshape(-1))
+    h_all = h_all.pin_memory()
+    d_in = torch.empty(max(B_max, 1024) * in_bytes, dtype=torch.uint8, device=dev)
+    d_out = torch.empty(max(B_max, 1024) * out_px * 4, dtype=torch.uint8, device=dev)
+    d_lab = torch.empty(max(B_max, 1024) * W * H, dtype=torch.int32, device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    pct = lambda v, q: round(float(v[min(len(v) - 1, int(q * len(v)))]), 4)
+
+    def measure(b, calls, run):
+        marks = [(ev(), ev()) for _ in range(calls)]
+        for k in range(3):
+            run(k % max(1, (1024 // b)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(calls):
+            a, e = marks[k]
+            a.record(stream)
+            run(k % max(1, (1024 // b)))
+            e.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        lat = sorted(a.elapsed_time(e) for a, e in marks)
+        return {"frames_per_s": round(b * calls / wall, 1), "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                "calls": calls}
+
+    ctx1 = depix.Context(W * H, 1)
+
+    def plain(slot):
+        d = d_in[slot * in_bytes:(slot + 1) * in_bytes]
+        d.copy_(h_all[slot * in_bytes:(slot + 1) * in_bytes], non_blocking=True)
+        ctx1.frame(d, W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out[slot * out_px * 4:], None, d_lab[slot * W * H:],
+                   stream=stream)
+
+    out = {"definition": "frame latency = its call's time from the start of the upload of the call's frames "
+                         "(pinned host -> device) to the end of its last kernel; frames/s over back-to-back calls",
+           "plain": dict(measure(1, n_frames, plain), batch=1)}
+    out["plain"]["frames"] = n_frames
+    rows = []
+    for b in (8, 32, 128, 1024):
+        if b > ctx.max_frames:
+            continue
+        ws_b, hs_b = np.full(b, W, np.int32), np.full(b, H, np.int32)
+        io = np.arange(b, dtype=np.uint64) * np.uint64(in_bytes)
+        oo = np.arange(b, dtype=np.uint64) * np.uint64(out_px * 4)
+
+        def batched(slot, b=b, ws_b=ws_b, hs_b=hs_b, io=io, oo=oo):
+            base = slot * b
+            d_in[base * in_bytes:(base + b) * in_bytes].copy_(h_all[base * in_bytes:(base + b) * in_bytes],
+                                                              non_blocking=True)
+            ctx.batch(ws_b, hs_b, io, oo, d_in[base * in_bytes:], p, d_out[base * out_px * 4:], d_lab[base * W * H:],
+                      stream=stream)
+
+        calls = max(8, min(200, (n_frames * 4) // b))
+        r = measure(b, calls, batched)
+        r["batch"] = b
+        r["beats_plain_frames_per_s"] = r["frames_per_s"] > out["plain"]["frames_per_s"]
+        r["p99_under_1ms"] = r["p99_ms"] < 1.0
+        rows.append(r)
+    ctx1.close()
+    out["batched"] = rows
+    ok = [r["batch"] for r in rows if r["beats_plain_frames_per_s"] and r["p99_under_1ms"]]
+    out["batches_beating_plain_with_p99_under_1ms"] = ok
+    return out
 
 
 def run_large(args, dev, stream):
@@ -754,25 +874,25 @@ def run_stream(args, dev, stream):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    cores = cpu_setup()
+    cores, kind = cpu_setup()
     frames = make_frames(min(DISTINCT, max(cores, 8)))
     per_step = cores
     for _ in range(max(args.warmup, 1)):
-        cpu_run(frames, per_step, cores)
+        cpu_run(frames, per_step, cores, kind)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cpu_run(frames, per_step, cores)
+        cpu_run(frames, per_step, cores, kind)
     dt = time.perf_counter() - t0
     value = per_step * args.steps / dt
-    sample = (f"{per_step} frames per step ({cores} threads, one frame each) through the CPU oracle: "
-              f"oracle/depix_oracle.c restates the reference's per-pixel stage bodies; the reference's own "
-              f"sources are not on this machine, so the restatement stands in for them")
+    sample = f"{per_step} frames per step ({cores} threads, one frame each): " + CPU_SAMPLE[kind]
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded generator)", "config": workload_config(per_step),
-            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if kind == "reference":
+        line["cpu_baseline"]["single_thread_value"] = round(cpu_run(frames, 2, 1, kind), 2)
     print(json.dumps(line))
 
 

@@ -54,6 +54,21 @@ typedef enum depix_layout {
     DEPIX_LAYOUT_RGBA = 1
 } depix_layout;
 
+/* How the luma y of the packed Y/U/V word is evaluated. The reference
+ * computes y = int(0.299 r + 0.587 g + 0.114 b) in double
+ * (graph_functions.cu:90); its two builds round that sum differently for
+ * 2490 of the 2^24 colours (42 of them grey levels), all with an exact
+ * integer sum, where one build's y is one below the other's. */
+typedef enum depix_yuv {
+    /* the reference's CUDA build (depixel_gpu.pro, nvcc with its default FMA
+     * contraction): fma(0.114, b, fma(0.299, r, 0.587 g)). The parity target
+     * of the frame path and the default. */
+    DEPIX_YUV_CUDA = 0,
+    /* the reference's stage bodies built for the host CPU: IEEE double with no
+     * contraction, (0.299 r + 0.587 g) + 0.114 b */
+    DEPIX_YUV_HOST = 1
+} depix_yuv;
+
 typedef struct depix_params {
     /* similarity thresholds in units of the packed Y/U/V byte fields
      * (graph_functions.cu:11-19): defaults Y 48, U 7, V 6; the reference's
@@ -68,6 +83,7 @@ typedef struct depix_params {
      * block) and islands, the diagonal with fewer votes removed, both on a
      * tie. Not in the reference; no parity target beyond the oracle. */
     int vote;
+    int yuv; /* depix_yuv: arithmetic of the luma (default DEPIX_YUV_CUDA) */
 } depix_params;
 
 void depix_default_params(depix_params* p);
@@ -82,9 +98,25 @@ depix_status depix_init_device(void);
 /* Sticky device-side faults of the current device since the last call,
  * then cleared: a bounded wait for a TMA tile load gave up and that tile
  * was left unwritten, bit 0 in the raster, bit 1 in the graph stage, bit 2
- * in the heuristics stage.
- * Synchronous. */
+ * in the heuristics stage. Returns DEPIX_ERR_TIMEOUT when any bit is set
+ * (the outputs of the launches since the last call are then incomplete),
+ * DEPIX_OK otherwise. Synchronous. */
 depix_status depix_take_device_faults(int* flags);
+
+/* Testing hooks: fault injection for the error paths, not for production.
+ *  - depix_debug_fail_allocations(after): after `after` more device
+ *    allocations by the library succeed, every later one fails (without
+ *    calling cudaMalloc) until called again with after < 0;
+ *  - depix_debug_live_allocations: device allocations the library holds now
+ *    (context scratch and staging, per-device tables, queue descriptors,
+ *    refiner buffers);
+ *  - depix_debug_tma_timeout(1): the TMA graph kernel issues no tile load
+ *    and gives up its bounded wait after a few polls, with nothing in flight,
+ *    so a frame's graph stage fails the way a lost load would: bit 1 of
+ *    depix_take_device_faults and DEPIX_ERR_TIMEOUT. (0) restores it. */
+depix_status depix_debug_fail_allocations(int after);
+depix_status depix_debug_live_allocations(long long* count);
+depix_status depix_debug_tma_timeout(int enable);
 
 /* ---------------------------------------------------------------------
  * Stage entry points: each mirrors one reference kernel, on device memory.
@@ -175,8 +207,9 @@ depix_status depix_raster(const uint8_t* d_img, int w, int h, int widthstep, dep
 
 /* Diagnostics. The packed Y/U/V word the graph stage compares (RGBtoYUV,
  * graph_functions.cu:80-131) for n pixels of 3 bytes in the reference's
- * memory order (d_px3: 3n bytes, d_words: n uint32). */
-depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, depix_stream s);
+ * memory order (d_px3: 3n bytes, d_words: n uint32), with the luma
+ * arithmetic yuv (depix_yuv). */
+depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, int yuv, uint32_t* d_words, depix_stream s);
 
 /* Copies the per-device cell-pattern tables to host arrays of 4096 entries
  * each: hull (count in bits 0-3, then 8 vertices of 6 bits: x+1 | (y+1)<<3
@@ -341,7 +374,7 @@ typedef struct depix_point { float x, y; } depix_point; /* Point, point.cu:2-11 
  * float2 / uchar4; img_data is a host BGR image (stride img_widthstep);
  * edge_count_h (w*h int) and graph_h (w*h bytes) are host outputs; time is
  * unused; p NULL means the reference build's thresholds (Y 5, U 7, V 6) and
- * p->subdivide / p->scale are ignored. Returns a malloc'd host array of
+ * luma arithmetic (DEPIX_YUV_CUDA); p->subdivide / p->scale are ignored. Returns a malloc'd host array of
  * w*h*45 points (the triangulated cells, unused slots (-100,-100)) that the
  * caller frees, or NULL on error (see depix_last_error). Synchronous; scratch
  * is kept per process between calls and guarded by a lock. */

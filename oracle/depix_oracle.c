@@ -30,15 +30,31 @@ static const int DJ[8] = {1, 1, 1, 0, 0, -1, -1, -1};
 
 /* ---------------------------------------------------------------- graph */
 
+/* Luma arithmetic modes (the library's depix_yuv): the reference's CUDA
+ * build contracts y's double sum into fused multiply-adds (nvcc's default,
+ * depixel_gpu.pro:48); its host build rounds every product and sum. */
+#define ORC_YUV_CUDA 0
+#define ORC_YUV_HOST 1
+
 /* Packed YUV word of one pixel given its three bytes in memory order.
  * Restates DATAtoINT + RGBtoYUV (graph_functions.cu:80-131): the first byte
- * plays "r", the third "b"; y in double, u/v in float, truncation toward zero,
- * negative u/v borrow into the higher fields. */
-uint32_t orc_yuv_word(uint8_t b0, uint8_t b1, uint8_t b2)
+ * plays "r", the third "b"; y in double (graph_functions.cu:90), u/v in
+ * float, truncation toward zero, negative u/v borrow into the higher fields.
+ * mode ORC_YUV_CUDA: y = fma(0.114, b, fma(0.299, r, 0.587 g)), the order
+ * the CUDA build evaluates (all 2^24 words equal that build's, measured on
+ * the GPU); ORC_YUV_HOST: (0.299 r + 0.587 g) + 0.114 b, each operation
+ * rounded (this file is compiled with -ffp-contract=off). */
+uint32_t orc_yuv_word(uint8_t b0, uint8_t b1, uint8_t b2, int mode)
 {
     int r = b0, g = b1, b = b2;
-    double yd = 0.299 * (double)(float)r + 0.587 * (double)(float)g;
-    yd = yd + 0.114 * (double)(float)b;
+    double R = (double)(float)r, G = (double)(float)g, B = (double)(float)b;
+    double yd;
+    if (mode == ORC_YUV_HOST) {
+        yd = 0.299 * R + 0.587 * G;
+        yd = yd + 0.114 * B;
+    } else {
+        yd = fma(0.114, B, fma(0.299, R, 0.587 * G));
+    }
     int y = (int)yd;
     int u = (int)((float)(b - y) * 0.492f);
     int v = (int)((float)(r - y) * 0.877f);
@@ -46,9 +62,9 @@ uint32_t orc_yuv_word(uint8_t b0, uint8_t b1, uint8_t b2)
 }
 
 /* Bulk form over n pixels of 3 bytes each. */
-void orc_yuv_words(const uint8_t* px, long n, uint32_t* out)
+void orc_yuv_words(const uint8_t* px, long n, int mode, uint32_t* out)
 {
-    for (long k = 0; k < n; k++) out[k] = orc_yuv_word(px[3 * k], px[3 * k + 1], px[3 * k + 2]);
+    for (long k = 0; k < n; k++) out[k] = orc_yuv_word(px[3 * k], px[3 * k + 1], px[3 * k + 2], mode);
 }
 
 /* Similarity test of two words (graph_functions.cu:291-293): every masked
@@ -64,13 +80,13 @@ static int similar_words(uint32_t a, uint32_t b, int tr_y, int tr_u, int tr_v)
 /* Similarity graph (graph_Kernel, kernel.cu:140-159 + diff,
  * graph_functions.cu:147-311): bit e set iff the neighbour in direction e
  * lies inside the image and is similar. */
-void orc_graph(const uint8_t* bgr, int w, int h, int ws, int tr_y, int tr_u, int tr_v, uint8_t* graph)
+void orc_graph(const uint8_t* bgr, int w, int h, int ws, int tr_y, int tr_u, int tr_v, int mode, uint8_t* graph)
 {
     uint32_t* words = (uint32_t*)malloc((size_t)w * h * sizeof(uint32_t));
     for (int j = 0; j < h; j++)
         for (int i = 0; i < w; i++) {
             const uint8_t* p = bgr + (size_t)j * ws + 3 * i;
-            words[j * w + i] = orc_yuv_word(p[0], p[1], p[2]);
+            words[j * w + i] = orc_yuv_word(p[0], p[1], p[2], mode);
         }
     for (int j = 0; j < h; j++)
         for (int i = 0; i < w; i++) {
@@ -992,7 +1008,7 @@ int orc_border_walks(const uint8_t* g, int w, int h, int32_t* nodes, int8_t* edg
 /* Runs the whole path on one BGR frame with the same outputs as the
  * reference driver (kernel.cu:286-526). Any output may be NULL. Returns the
  * number of cells whose ear clip failed. */
-int orc_frame(const uint8_t* bgr, int w, int h, int ws, int subdivide, int tr_y, int tr_u, int tr_v,
+int orc_frame(const uint8_t* bgr, int w, int h, int ws, int subdivide, int tr_y, int tr_u, int tr_v, int mode,
               const uint8_t* graph_in, uint8_t* graph_trivial_out, uint8_t* graph_resolved_out, int* ec_cells_out,
               float* diag_cells_out, int* ec_final_out, float* diag_final_out, float* pos_out, uint8_t* col_out)
 {
@@ -1003,7 +1019,7 @@ int orc_frame(const uint8_t* bgr, int w, int h, int ws, int subdivide, int tr_y,
         memcpy(g0, graph_in, n);
         memcpy(g1, graph_in, n);
     } else {
-        orc_graph(bgr, w, h, ws, tr_y, tr_u, tr_v, g0);
+        orc_graph(bgr, w, h, ws, tr_y, tr_u, tr_v, mode, g0);
         orc_trivial(g0, w, h);
         orc_heuristics(g0, w, h, g1);
     }

@@ -16,6 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libdepix_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 CELL = 45
+# luma arithmetic of the packed Y/U/V word (the library's depix_yuv): the
+# reference's CUDA build (fused multiply-adds) or its host build
+YUV_CUDA = 0
+YUV_HOST = 1
 
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -42,9 +46,9 @@ def lib():
         build()
         L = ctypes.CDLL(LIB_PATH)
         L.orc_yuv_word.restype = ctypes.c_uint32
-        L.orc_yuv_word.argtypes = [ctypes.c_uint8] * 3
+        L.orc_yuv_word.argtypes = [ctypes.c_uint8] * 3 + [ctypes.c_int]
         L.orc_graph.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                ctypes.c_int, _u8p]
+                                ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_trivial.argtypes = [_u8p, ctypes.c_int, ctypes.c_int]
         L.orc_heuristics.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u8p]
         L.orc_heuristics_vote.argtypes = [_u8p, ctypes.c_int, ctypes.c_int, _u8p]
@@ -57,7 +61,7 @@ def lib():
         vp = ctypes.c_void_p
         L.orc_frame.restype = ctypes.c_int
         L.orc_frame.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                ctypes.c_int, ctypes.c_int] + [vp] * 9
+                                ctypes.c_int, ctypes.c_int, ctypes.c_int] + [vp] * 9
         _lib = L
     return _lib
 
@@ -87,26 +91,28 @@ class Frame:
                 _ptr(self.ec), _ptr(self.diag), _ptr(self.pos), _ptr(self.col)]
 
 
-def frame(bgr, w, h, ws, subdivide=True, tr=(48, 7, 6), graph_in=None) -> Frame:
-    """Run the oracle's whole path on a reference-layout BGR buffer."""
+def frame(bgr, w, h, ws, subdivide=True, tr=(48, 7, 6), graph_in=None, yuv=YUV_CUDA) -> Frame:
+    """Run the oracle's whole path on a reference-layout BGR buffer (luma
+    arithmetic of the reference's CUDA build unless yuv=YUV_HOST)."""
     bgr = np.ascontiguousarray(bgr, np.uint8)
     f = Frame(w, h)
     gi = None if graph_in is None else np.ascontiguousarray(graph_in, np.uint8)
-    f.fails = lib().orc_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), tr[0], tr[1], tr[2], _ptr(gi), *f._args())
+    f.fails = lib().orc_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), tr[0], tr[1], tr[2], int(yuv), _ptr(gi),
+                              *f._args())
     return f
 
 
-def yuv_word(b0, b1, b2) -> int:
-    return int(lib().orc_yuv_word(b0, b1, b2))
+def yuv_word(b0, b1, b2, yuv=YUV_CUDA) -> int:
+    return int(lib().orc_yuv_word(b0, b1, b2, int(yuv)))
 
 
-def graph(bgr, w, h, ws, tr=(48, 7, 6), vote=False):
+def graph(bgr, w, h, ws, tr=(48, 7, 6), vote=False, yuv=YUV_CUDA):
     """Similarity graph, then trivial and heuristic resolution (the
     reference's ordered tests, or the weighted vote): returns
     (raw, after_trivial, resolved)."""
     bgr = np.ascontiguousarray(bgr, np.uint8)
     raw = np.zeros(w * h, np.uint8)
-    lib().orc_graph(bgr, w, h, ws, tr[0], tr[1], tr[2], raw)
+    lib().orc_graph(bgr, w, h, ws, tr[0], tr[1], tr[2], int(yuv), raw)
     triv = raw.copy()
     lib().orc_trivial(triv, w, h)
     return raw, triv, heuristics(triv, w, h, vote)
@@ -186,15 +192,92 @@ def ref_frame(bgr, w, h, ws, subdivide=True, tr_y=48, graph_in=None) -> Frame:
     return f
 
 
-def yuv_words(px3: np.ndarray, ref_tr_y: int = 0) -> np.ndarray:
-    """Packed YUV words of an (n, 3) byte array; with ref_tr_y set, computed
-    by the reference's own functions instead of the oracle's."""
+def ref_frame_vbo(bgr, w, h, ws, subdivide=True, tr_y=48):
+    """The reference's host build on one frame, returning only what the frame
+    path hands on (resolved graph, VBO positions and colours)."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    n = w * h
+    graph = np.zeros(n, np.uint8)
+    pos = np.zeros(n * CELL * 2, np.float32)
+    col = np.zeros(n * CELL * 4, np.uint8)
+    ref_lib(tr_y).ref_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), None, None, _ptr(graph), None, None, None,
+                            None, _ptr(pos), _ptr(col))
+    return graph, pos, col
+
+
+def build_ref(gpu: bool = False) -> bool:
+    """Runs oracle/build_ref.sh (host build only unless gpu) and reports
+    whether the host build of the reference's stage bodies is present."""
+    env = dict(os.environ)
+    if not gpu:
+        env["DEPIX_REF_NO_GPU"] = "1"
+    subprocess.run([os.path.join(HERE, "build_ref.sh")], env=env, check=False, stdout=subprocess.DEVNULL)
+    return ref_available(5) and ref_available(48)
+
+
+def yuv_words(px3: np.ndarray, ref_tr_y: int = 0, yuv=YUV_CUDA) -> np.ndarray:
+    """Packed YUV words of an (n, 3) byte array by the oracle (luma
+    arithmetic yuv); with ref_tr_y set, computed by the reference's own
+    functions in its host build instead."""
     px3 = np.ascontiguousarray(px3, np.uint8)
     n = px3.shape[0]
     out = np.zeros(n, np.uint32)
-    L = ref_lib(ref_tr_y) if ref_tr_y else lib()
-    fn = L.ref_yuv_words if ref_tr_y else L.orc_yuv_words
-    fn.restype = None
-    fn.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
-    fn(_ptr(px3), n, _ptr(out))
+    if ref_tr_y:
+        fn = ref_lib(ref_tr_y).ref_yuv_words
+        fn.restype = None
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p]
+        fn(_ptr(px3), n, _ptr(out))
+    else:
+        fn = lib().orc_yuv_words
+        fn.restype = None
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_void_p]
+        fn(_ptr(px3), n, int(yuv), _ptr(out))
+    return out
+
+
+# ------------------------------------------------------ reference CUDA build
+
+_refgpu = {}
+
+
+def refgpu_available(tr_y: int) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libdepix_refgpu{tr_y}.so"))
+
+
+def refgpu_lib(tr_y: int):
+    """The reference's own stage bodies built for the GPU with its own device
+    flags (oracle/ref_gpu.cu; Y threshold 5 or 48). Needs a CUDA device."""
+    if tr_y not in _refgpu:
+        L = ctypes.CDLL(os.path.join(REF_DIR, f"libdepix_refgpu{tr_y}.so"))
+        vp = ctypes.c_void_p
+        L.refgpu_frame.restype = ctypes.c_int
+        L.refgpu_frame.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [vp] * 9
+        L.refgpu_yuv_words.restype = ctypes.c_int
+        L.refgpu_yuv_words.argtypes = [vp]
+        L.refgpu_last_error.restype = ctypes.c_char_p
+        _refgpu[tr_y] = L
+    return _refgpu[tr_y]
+
+
+def _refgpu_check(L, rc):
+    if rc != 0:
+        raise RuntimeError("reference CUDA build: " + L.refgpu_last_error().decode())
+
+
+def refgpu_frame(bgr, w, h, ws, subdivide=True, tr_y=48, graph_in=None) -> Frame:
+    """All stage outputs of one frame from the reference's CUDA build."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    f = Frame(w, h)
+    gi = None if graph_in is None else np.ascontiguousarray(graph_in, np.uint8)
+    L = refgpu_lib(tr_y)
+    _refgpu_check(L, L.refgpu_frame(_ptr(bgr), w, h, ws, int(bool(subdivide)), _ptr(gi), *f._args()))
+    return f
+
+
+def refgpu_yuv_words(tr_y: int = 5) -> np.ndarray:
+    """The packed YUV word of every byte triple b0 | b1 << 8 | b2 << 16 (2^24
+    entries) as the reference's CUDA build computes it."""
+    out = np.zeros(1 << 24, np.uint32)
+    L = refgpu_lib(tr_y)
+    _refgpu_check(L, L.refgpu_yuv_words(_ptr(out)))
     return out

@@ -4,9 +4,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h> // header-only: ranges cost a pointer test unless a profiler is attached
 
 #include "depix_internal.h"
 
@@ -19,6 +22,31 @@ thread_local std::string t_last_error;
 }  // namespace
 
 void depix::set_last_error(const std::string& msg) { t_last_error = msg; }
+
+namespace {
+std::atomic<long long> g_live_allocs{0};
+std::atomic<int> g_fail_after{-1}; // < 0: never; n: n more allocations succeed, then all fail
+}  // namespace
+
+cudaError_t depix::dev_alloc(void** p, size_t bytes)
+{
+    *p = nullptr;
+    int f = g_fail_after.load();
+    while (f >= 0) {
+        if (f == 0) return cudaErrorMemoryAllocation;
+        if (g_fail_after.compare_exchange_weak(f, f - 1)) break;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) g_live_allocs++;
+    else cudaGetLastError();
+    return e;
+}
+
+void depix::dev_free(void* p)
+{
+    if (!p) return;
+    if (cudaFree(p) == cudaSuccess) g_live_allocs--;
+}
 
 namespace {
 
@@ -102,8 +130,7 @@ depix_status scale_table(int scale, cudaStream_t user, const uint32_t** out)
         }
     }
     uint32_t* lut = nullptr;
-    if (cudaMalloc(&lut, scale_mask_words(scale) * sizeof(uint32_t)) != cudaSuccess) {
-        cudaGetLastError();
+    if (dev_alloc(&lut, scale_mask_words(scale) * sizeof(uint32_t)) != cudaSuccess) {
         t_last_error = "cudaMalloc of the scale table failed";
         return DEPIX_ERR_ALLOC;
     }
@@ -113,7 +140,7 @@ depix_status scale_table(int scale, cudaStream_t user, const uint32_t** out)
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     if (e != cudaSuccess) {
-        cudaFree(lut);
+        dev_free(lut);
         return cuda_fail(e, "build_scale_masks");
     }
     v[scale] = lut;
@@ -149,6 +176,7 @@ depix_status check_params(const depix_params* p)
     if (p->scale < 1 || p->scale > 64) return arg_fail("scale must be in 1..64");
     if (p->tr_y < 0 || p->tr_u < 0 || p->tr_v < 0) return arg_fail("thresholds must be >= 0");
     if (p->vote != 0 && p->vote != 1) return arg_fail("vote must be 0 or 1");
+    if (p->yuv != DEPIX_YUV_CUDA && p->yuv != DEPIX_YUV_HOST) return arg_fail("yuv must be DEPIX_YUV_CUDA or DEPIX_YUV_HOST");
     return DEPIX_OK;
 }
 
@@ -191,6 +219,7 @@ void depix_default_params(depix_params* p)
     p->subdivide = 1;
     p->scale = 4;
     p->vote = 0;
+    p->yuv = DEPIX_YUV_CUDA;
 }
 
 const char* depix_status_string(depix_status s)
@@ -221,6 +250,31 @@ depix_status depix_take_device_faults(int* flags)
     DEPIX_CK(take_graph_fault(&graph));
     DEPIX_CK(take_heuristics_fault(&heur));
     *flags = (raster ? 1 : 0) | (graph ? 2 : 0) | (heur ? 4 : 0);
+    if (*flags) {
+        t_last_error = "a bounded device-side wait for a TMA tile load gave up; the tiles of those blocks were "
+                       "left unwritten";
+        return DEPIX_ERR_TIMEOUT;
+    }
+    return DEPIX_OK;
+}
+
+depix_status depix_debug_fail_allocations(int after)
+{
+    g_fail_after.store(after < 0 ? -1 : after);
+    return DEPIX_OK;
+}
+
+depix_status depix_debug_live_allocations(long long* count)
+{
+    if (!count) return arg_fail("NULL count");
+    *count = g_live_allocs.load();
+    return DEPIX_OK;
+}
+
+depix_status depix_debug_tma_timeout(int enable)
+{
+    DEPIX_TRY(ensure_tables(nullptr));
+    DEPIX_CK(set_graph_tma_timeout_test(enable));
     return DEPIX_OK;
 }
 
@@ -231,7 +285,7 @@ depix_status depix_graph(const uint8_t* d_img, int w, int h, int widthstep, depi
     DEPIX_TRY(check_params(p));
     if (!d_graph) return arg_fail("graph pointer is NULL");
     FrameBatch b{d_img, 0, d_graph, 0, w, h, widthstep, (int)layout};
-    DEPIX_CK(launch_graph(b, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), fuse_trivial != 0, S(s)));
+    DEPIX_CK(launch_graph(b, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv), fuse_trivial != 0, S(s)));
     return DEPIX_OK;
 }
 
@@ -323,10 +377,11 @@ depix_status depix_border_walks(const uint8_t* d_graph, int w, int h, int nframe
     return DEPIX_OK;
 }
 
-depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, uint32_t* d_words, depix_stream s)
+depix_status depix_yuv_words(const uint8_t* d_px3, size_t n, int yuv, uint32_t* d_words, depix_stream s)
 {
     if (n && (!d_px3 || !d_words)) return arg_fail("NULL pointer");
-    DEPIX_CK(launch_yuv_words(d_px3, n, d_words, S(s)));
+    if (yuv != DEPIX_YUV_CUDA && yuv != DEPIX_YUV_HOST) return arg_fail("yuv must be DEPIX_YUV_CUDA or DEPIX_YUV_HOST");
+    DEPIX_CK(launch_yuv_words(d_px3, n, yuv, d_words, S(s)));
     return DEPIX_OK;
 }
 
@@ -403,7 +458,11 @@ struct depix_context {
 
 namespace {
 
-// Brackets one stage's launches with events when the context is timing.
+const char* const kStageName[DEPIX_STAGE_COUNT] = {"depix graph", "depix heuristics", "depix labels",
+                                                   "depix raster"};
+
+// Brackets one stage's launches with an NVTX range (host side, seen by
+// profilers) and, when the context is timing, with CUDA events.
 struct StageTimer {
     depix_context* c;
     int stage, launches;
@@ -412,6 +471,7 @@ struct StageTimer {
     StageTimer(depix_context* c_, int stage_, int launches_, cudaStream_t s_)
         : c(c_), stage(stage_), launches(launches_), s(s_)
     {
+        nvtxRangePushA(kStageName[stage]);
         if (c->timing) {
             a = c->take_event();
             cudaEventRecord(a, s);
@@ -419,6 +479,7 @@ struct StageTimer {
     }
     ~StageTimer()
     {
+        nvtxRangePop();
         if (!c->timing || !a) return;
         cudaEvent_t b = c->take_event();
         cudaEventRecord(b, s);
@@ -437,33 +498,30 @@ depix_status ctx_raster(depix_context* c, const RasterBatch& rb, int nframes, cu
 depix_status ensure_staging(depix_context* c, size_t in_bytes, size_t out_bytes, size_t labels)
 {
     if (in_bytes > c->stage_in_bytes) {
-        cudaFree(c->stage_in);
+        dev_free(c->stage_in);
         c->stage_in = nullptr;
         c->stage_in_bytes = 0;
-        if (cudaMalloc(&c->stage_in, in_bytes) != cudaSuccess) {
-            cudaGetLastError();
+        if (dev_alloc(&c->stage_in, in_bytes) != cudaSuccess) {
             t_last_error = "cudaMalloc of input staging failed";
             return DEPIX_ERR_ALLOC;
         }
         c->stage_in_bytes = in_bytes;
     }
     if (out_bytes > c->stage_out_bytes) {
-        cudaFree(c->stage_out);
+        dev_free(c->stage_out);
         c->stage_out = nullptr;
         c->stage_out_bytes = 0;
-        if (cudaMalloc(&c->stage_out, out_bytes) != cudaSuccess) {
-            cudaGetLastError();
+        if (dev_alloc(&c->stage_out, out_bytes) != cudaSuccess) {
             t_last_error = "cudaMalloc of output staging failed";
             return DEPIX_ERR_ALLOC;
         }
         c->stage_out_bytes = out_bytes;
     }
     if (labels > c->stage_label_count) {
-        cudaFree(c->stage_labels);
+        dev_free(c->stage_labels);
         c->stage_labels = nullptr;
         c->stage_label_count = 0;
-        if (cudaMalloc(&c->stage_labels, labels * sizeof(int32_t)) != cudaSuccess) {
-            cudaGetLastError();
+        if (dev_alloc(&c->stage_labels, labels * sizeof(int32_t)) != cudaSuccess) {
             t_last_error = "cudaMalloc of label staging failed";
             return DEPIX_ERR_ALLOC;
         }
@@ -506,7 +564,7 @@ depix_status run_batch(depix_context* ctx, int n, const int* w, const int* h, co
                        const uint64_t* out_offset, const uint8_t* d_img, const depix_params* p, uint8_t* d_out,
                        int32_t* d_labels, const BatchShape& shape, cudaStream_t s)
 {
-    const uint32_t thr = pack_thresholds(p->tr_y, p->tr_u, p->tr_v);
+    const uint32_t thr = pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv);
     if (shape.uniform && shape.strided) {
         // equal sizes at equal strides: one launch per stage for the batch
         size_t px = (size_t)w[0] * h[0];
@@ -674,11 +732,10 @@ depix_status depix_context_create(depix_context** out, size_t max_pixels, int ma
     c->max_pixels = max_pixels;
     c->max_frames = max_frames;
     size_t bytes = max_pixels * (size_t)max_frames;
-    if (cudaMalloc(&c->graph_a, bytes) != cudaSuccess || cudaMalloc(&c->graph_b, bytes) != cudaSuccess) {
-        cudaFree(c->graph_a);
+    if (dev_alloc(&c->graph_a, bytes) != cudaSuccess || dev_alloc(&c->graph_b, bytes) != cudaSuccess) {
+        dev_free(c->graph_a);
         delete c;
         t_last_error = "cudaMalloc of context scratch failed";
-        cudaGetLastError();
         return DEPIX_ERR_ALLOC;
     }
     *out = c;
@@ -688,11 +745,11 @@ depix_status depix_context_create(depix_context** out, size_t max_pixels, int ma
 depix_status depix_context_destroy(depix_context* c)
 {
     if (!c) return DEPIX_OK;
-    cudaFree(c->graph_a);
-    cudaFree(c->graph_b);
-    cudaFree(c->stage_in);
-    cudaFree(c->stage_out);
-    cudaFree(c->stage_labels);
+    dev_free(c->graph_a);
+    dev_free(c->graph_b);
+    dev_free(c->stage_in);
+    dev_free(c->stage_out);
+    dev_free(c->stage_labels);
     if (c->queue) queue_runner_destroy(c->queue);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
@@ -784,7 +841,7 @@ depix_status depix_frame(depix_context* ctx, const uint8_t* d_img, int w, int h,
     {
         StageTimer t(ctx, DEPIX_STAGE_GRAPH, 1, s);
         FrameBatch gb{d_img, 0, ctx->graph_a, 0, w, h, widthstep, (int)layout};
-        DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+        DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv), true, s));
     }
     {
         StageTimer t(ctx, DEPIX_STAGE_HEURISTICS, 1, s);
@@ -832,8 +889,11 @@ depix_status depix_batch_host(depix_context* ctx, int n, const int* w, const int
     DEPIX_TRY(check_batch(ctx, n, w, h, in_offset, out_offset, shape));
     for (int k = 0; k < n; k++) DEPIX_TRY(check_out_size(w[k], h[k], p));
     for (int k = 0; k < n; k++) {
+        // compared without forming offset + size, which a corrupt offset
+        // near 2^64 would wrap around
         size_t ib = (size_t)w[k] * h[k] * 4, ob = ib * (size_t)p->scale * p->scale;
-        if (in_offset[k] + ib > in_bytes || out_offset[k] + ob > out_bytes)
+        if (in_offset[k] > in_bytes || ib > in_bytes - in_offset[k] || out_offset[k] > out_bytes ||
+            ob > out_bytes - out_offset[k])
             return arg_fail("a frame lies outside the host buffers");
     }
     DEPIX_TRY(ensure_staging(ctx, in_bytes, out_bytes, h_labels ? shape.total_pixels : 0));
@@ -872,19 +932,19 @@ struct CompatScratch {
     int* ec_snap = nullptr;
     void release()
     {
-        cudaFree(img); cudaFree(g0); cudaFree(g1); cudaFree(diag); cudaFree(snap); cudaFree(ec); cudaFree(ec_snap);
+        dev_free(img); dev_free(g0); dev_free(g1); dev_free(diag); dev_free(snap); dev_free(ec); dev_free(ec_snap);
         *this = CompatScratch();
     }
     bool reserve(size_t ib, size_t px)
     {
         if (ib <= img_bytes && px <= pixels && img) return true;
         release();
-        bool ok = cudaMalloc(&img, ib) == cudaSuccess && cudaMalloc(&g0, px) == cudaSuccess &&
-                  cudaMalloc(&g1, px) == cudaSuccess &&
-                  cudaMalloc(&diag, px * kCell * sizeof(float2)) == cudaSuccess &&
-                  cudaMalloc(&snap, px * kCell * sizeof(float2)) == cudaSuccess &&
-                  cudaMalloc(&ec, px * sizeof(int)) == cudaSuccess &&
-                  cudaMalloc(&ec_snap, px * sizeof(int)) == cudaSuccess;
+        bool ok = dev_alloc(&img, ib) == cudaSuccess && dev_alloc(&g0, px) == cudaSuccess &&
+                  dev_alloc(&g1, px) == cudaSuccess &&
+                  dev_alloc(&diag, px * kCell * sizeof(float2)) == cudaSuccess &&
+                  dev_alloc(&snap, px * kCell * sizeof(float2)) == cudaSuccess &&
+                  dev_alloc(&ec, px * sizeof(int)) == cudaSuccess &&
+                  dev_alloc(&ec_snap, px * sizeof(int)) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();
             release();
@@ -904,7 +964,7 @@ depix_status compat_run(void* pos, void* colorPos, char* img_data, int w, int h,
 {
     DEPIX_TRY(check_size(w, h));
     if (!img_data || ws < 3 * w) return arg_fail("bad host image");
-    depix_params ref{5, 7, 6, 0, 1, 0};
+    depix_params ref{5, 7, 6, 0, 1, 0, DEPIX_YUV_CUDA};
     if (!p) p = &ref;
     DEPIX_TRY(check_params(p));
     DEPIX_TRY(ensure_tables(nullptr));
@@ -918,7 +978,7 @@ depix_status compat_run(void* pos, void* colorPos, char* img_data, int w, int h,
     cudaStream_t s = 0;
     DEPIX_CK(cudaMemcpyAsync(c.img, img_data, ib, cudaMemcpyHostToDevice, s));
     FrameBatch gb{c.img, 0, c.g0, 0, w, h, ws, DEPIX_LAYOUT_BGR};
-    DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+    DEPIX_CK(launch_graph(gb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv), true, s));
     GraphBatch hb{c.g0, c.g1, 0, w, h, p->vote};
     DEPIX_CK(launch_heuristics(hb, 1, s));
     DEPIX_CK(launch_cells(c.g1, w, h, c.diag, c.ec, s));

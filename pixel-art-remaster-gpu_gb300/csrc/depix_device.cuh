@@ -42,16 +42,28 @@ __device__ __forceinline__ unsigned inside_mask(int x, int y, int w, int h)
 // Packed Y/U/V word of one pixel from its bytes in the reference's memory
 // order (b0 plays "r", b2 plays "b": RGBtoYUV + DATAtoINT,
 // graph_functions.cu:80-131). y is the truncated double 0.299 r + 0.587 g +
-// 0.114 b; off exact multiples of 1/1000 that equals the integer quotient of
-// 299 r + 587 g + 114 b by 1000, so the double evaluation (no contraction) is
-// only needed when the remainder is zero.
-__device__ __forceinline__ uint32_t yuv_word(int r, int g, int b)
+// 0.114 b, evaluated as one of the reference's two builds evaluates it
+// (depix_params.yuv):
+//  - DEPIX_YUV_CUDA: its CUDA build (nvcc contracts the sum into fused
+//    multiply-adds): fma(0.114, b, fma(0.299, r, 0.587 g));
+//  - DEPIX_YUV_HOST: its host build, IEEE with no contraction:
+//    (0.299 r + 0.587 g) + 0.114 b.
+// Off exact multiples of 1/1000 the sum is at least 0.001 away from an
+// integer, and either evaluation truncates to the integer quotient of
+// 299 r + 587 g + 114 b by 1000; only a zero remainder needs the double
+// evaluation, where the two builds differ for 2490 of the 2^24 colours.
+__device__ __forceinline__ uint32_t yuv_word(int r, int g, int b, int mode)
 {
     int s = 299 * r + 587 * g + 114 * b;
     int y = s / 1000;
     if (s - y * 1000 == 0) {
-        double t = __dadd_rn(__dmul_rn(0.299, (double)r), __dmul_rn(0.587, (double)g));
-        t = __dadd_rn(t, __dmul_rn(0.114, (double)b));
+        double t;
+        if (mode == DEPIX_YUV_HOST) {
+            t = __dadd_rn(__dmul_rn(0.299, (double)r), __dmul_rn(0.587, (double)g));
+            t = __dadd_rn(t, __dmul_rn(0.114, (double)b));
+        } else {
+            t = __fma_rn(0.114, (double)b, __fma_rn(0.299, (double)r, __dmul_rn(0.587, (double)g)));
+        }
         y = __double2int_rz(t);
     }
     int u = __float2int_rz(__fmul_rn((float)(b - y), 0.492f));
@@ -59,12 +71,17 @@ __device__ __forceinline__ uint32_t yuv_word(int r, int g, int b)
     return (uint32_t)(y * 65536 + u * 256 + v);
 }
 
-// thresholds packed like a word; a field threshold above 255 can never be exceeded
-__host__ __device__ __forceinline__ uint32_t pack_thresholds(int ty, int tu, int tv)
+// Thresholds packed like a word (a field threshold above 255 can never be
+// exceeded), with the y arithmetic (depix_params.yuv) in bits 24-31: the
+// similarity test ignores that byte, so the kernels that build words carry
+// the mode in the thresholds they already take.
+__host__ __device__ __forceinline__ uint32_t pack_thresholds(int ty, int tu, int tv, int yuv)
 {
     auto c = [](int t) { return (uint32_t)(t < 0 ? 0 : (t > 255 ? 255 : t)); };
-    return (c(ty) << 16) | (c(tu) << 8) | c(tv);
+    return ((uint32_t)(yuv & 0xFF) << 24) | (c(ty) << 16) | (c(tu) << 8) | c(tv);
 }
+
+__host__ __device__ __forceinline__ int yuv_mode_of(uint32_t thr) { return (int)(thr >> 24); }
 
 // similarity of two words: every masked field within its threshold
 // (graph_functions.cu:291-293)
@@ -85,9 +102,11 @@ __device__ __forceinline__ uint32_t load_bgr(const uint8_t* img, int ws, int lay
     return (uint32_t)__ldg(q) | ((uint32_t)__ldg(q + 1) << 8) | ((uint32_t)__ldg(q + 2) << 16);
 }
 
-__device__ __forceinline__ uint32_t word_of_bgr(uint32_t c)
+// word of packed bytes c = b0 | b1 << 8 | b2 << 16 under the y arithmetic
+// carried in the packed thresholds thr
+__device__ __forceinline__ uint32_t word_of_bgr(uint32_t c, uint32_t thr)
 {
-    return yuv_word((int)(c & 0xFF), (int)((c >> 8) & 0xFF), (int)((c >> 16) & 0xFF));
+    return yuv_word((int)(c & 0xFF), (int)((c >> 8) & 0xFF), (int)((c >> 16) & 0xFF), yuv_mode_of(thr));
 }
 
 // Byte at linear offset `off` of the reference's BGR image (rows `vws` bytes,
@@ -773,6 +792,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
             : "memory");
         if (done) return true;
     }
+    return false;
+}
+
+// Polls a block allows a TMA tile load before it gives up (about a second on
+// GB300 at most; a load completes in microseconds).
+constexpr int kTmaPolls = 1 << 22;
+
+// Waits for the tile load completing on bar. When the wait gives up, it sets
+// the stage's sticky fault flag and then waits again, bounded the same way,
+// for the load it issued, so that a load still in flight does not land in
+// shared memory after the block has left; the block then leaves its tile
+// unwritten. False when the first wait gave up.
+__device__ __forceinline__ bool tma_wait_or_flag(uint64_t* bar, int* fault, int polls = kTmaPolls)
+{
+    if (mbar_wait_bounded(bar, 0, polls)) return true;
+    atomicExch(fault, 1);
+    mbar_wait_bounded(bar, 0, polls);
     return false;
 }
 

@@ -864,8 +864,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
         // the box holds RGBA words; the tile works on the reference's byte
         // order (b0, b1, b2) = (B, G, R), as load_bgr gives it
         if (threadIdx.x == 0) {
-            M.tma_ok = mbar_wait_bounded(&M.bar, 0, 1 << 22) ? 1 : 0;
-            if (!M.tma_ok) atomicExch(&g_raster_fault, 1);
+            M.tma_ok = tma_wait_or_flag(&M.bar, &g_raster_fault) ? 1 : 0;
         }
         __syncthreads();
         if (!M.tma_ok) return;

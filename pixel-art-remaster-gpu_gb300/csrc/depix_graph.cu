@@ -16,6 +16,10 @@ namespace depix {
 // graph was left unwritten); read and cleared by depix_take_device_faults
 __device__ int g_graph_fault;
 __device__ int g_heur_fault; // the same for the heuristics stage
+// Test switch (depix_debug_tma_timeout): the TMA graph kernel issues no tile
+// load and its wait gives up after kTestPolls polls, with nothing in flight.
+__device__ int g_graph_tma_timeout_test;
+constexpr int kTestPolls = 16;
 
 constexpr int kGTW = 64;  // graph tile width (pixels)
 constexpr int kGTH = 16;  // graph tile height
@@ -37,11 +41,11 @@ __device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uin
         __shared__ uint64_t bar;
         __shared__ int ok;
         if (threadIdx.x == 0) {
+            const bool test_timeout = *(volatile int*)&g_graph_tma_timeout_test != 0;
             mbar_init(&bar, 1);
             mbar_expect_tx(&bar, (uint32_t)sizeof(box));
-            tma_load_3d(&box[0][0], pix_map, x0 - 4, y0 - 1, frame, &bar);
-            ok = mbar_wait_bounded(&bar, 0, 1 << 22) ? 1 : 0;
-            if (!ok) atomicExch(&g_graph_fault, 1);
+            if (!test_timeout) tma_load_3d(&box[0][0], pix_map, x0 - 4, y0 - 1, frame, &bar);
+            ok = tma_wait_or_flag(&bar, &g_graph_fault, test_timeout ? kTestPolls : kTmaPolls) ? 1 : 0;
         }
         __syncthreads();
         if (!ok) return;
@@ -51,14 +55,14 @@ __device__ __forceinline__ void graph_tile(const FrameRef f, int x0, int y0, uin
             // RGBA -> the reference's byte order (b0, b1, b2) = (B, G, R); zero outside the image
             const uint32_t c = ((p >> 16) & 0xFFu) | (p & 0xFF00u) | ((p & 0xFFu) << 16);
             const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
-            words[ry][rx] = (gx >= 0 && gy >= 0 && gx < w && gy < h) ? word_of_bgr(c) : 0u;
+            words[ry][rx] = (gx >= 0 && gy >= 0 && gx < w && gy < h) ? word_of_bgr(c, thr) : 0u;
         }
     } else {
         for (int k = threadIdx.x; k < RW * RH; k += blockDim.x) {
             int rx = k % RW, ry = k / RW;
             int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
             uint32_t wd = 0;
-            if (gx >= 0 && gy >= 0 && gx < w && gy < h) wd = word_of_bgr(load_bgr(f.img, f.ws, LAYOUT, gx, gy));
+            if (gx >= 0 && gy >= 0 && gx < w && gy < h) wd = word_of_bgr(load_bgr(f.img, f.ws, LAYOUT, gx, gy), thr);
             words[ry][rx] = wd;
         }
     }
@@ -319,8 +323,7 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
             mbar_init(&bar, 1);
             mbar_expect_tx(&bar, (uint32_t)sizeof(s));
             tma_load_3d(&s[0][0], map, ox, oy, frame, &bar);
-            ok = mbar_wait_bounded(&bar, 0, 1 << 22) ? 1 : 0;
-            if (!ok) atomicExch(&g_heur_fault, 1);
+            ok = tma_wait_or_flag(&bar, &g_heur_fault) ? 1 : 0;
         }
         __syncthreads();
         if (!ok) return;
@@ -768,20 +771,26 @@ int queue_blocks_per_sm(int stage, const QueueBatch& q)
     }
 }
 
-__global__ void k_yuv_words(const uint8_t* px3, size_t n, uint32_t* out)
+__global__ void k_yuv_words(const uint8_t* px3, size_t n, int mode, uint32_t* out)
 {
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    out[k] = yuv_word(px3[3 * k], px3[3 * k + 1], px3[3 * k + 2]);
+    out[k] = yuv_word(px3[3 * k], px3[3 * k + 1], px3[3 * k + 2], mode);
 }
 
 // ----------------------------------------------------------------- launch
 
-cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, uint32_t* out, cudaStream_t s)
+cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, int mode, uint32_t* out, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
-    k_yuv_words<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(px3, n, out);
+    k_yuv_words<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(px3, n, mode, out);
     return cudaGetLastError();
+}
+
+cudaError_t set_graph_tma_timeout_test(int on)
+{
+    int v = on ? 1 : 0;
+    return cudaMemcpyToSymbol(g_graph_tma_timeout_test, &v, sizeof(int));
 }
 
 cudaError_t take_graph_fault(int* out)

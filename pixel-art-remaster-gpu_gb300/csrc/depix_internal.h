@@ -176,7 +176,23 @@ cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, in
 cudaError_t launch_labels(const uint8_t* g, int32_t* labels, int w, int h, int nframes, size_t frame_stride,
                           cudaStream_t s);
 
-cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, uint32_t* out, cudaStream_t s);
+// Device allocations of the library's own scratch go through these two: a
+// count of live allocations, and fault injection for tests
+// (depix_debug_fail_allocations): an injected failure returns
+// cudaErrorMemoryAllocation without calling cudaMalloc.
+cudaError_t dev_alloc(void** p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_alloc(T** p, size_t bytes)
+{
+    return dev_alloc(reinterpret_cast<void**>(p), bytes);
+}
+void dev_free(void* p);
+// Test switch (depix_debug_tma_timeout): the TMA graph kernel issues no tile
+// load and gives up after a few polls, so its bounded wait's error path runs
+// with nothing in flight.
+cudaError_t set_graph_tma_timeout_test(int on);
+
+cudaError_t launch_yuv_words(const uint8_t* px3, size_t n, int mode, uint32_t* out, cudaStream_t s);
 
 // geometry stage
 cudaError_t init_tables(cudaStream_t s);

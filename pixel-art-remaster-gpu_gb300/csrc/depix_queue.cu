@@ -99,8 +99,8 @@ public:
         for (auto e : tev)
             if (e) cudaEventDestroy(e);
         if (capture_stream) cudaStreamDestroy(capture_stream);
-        cudaFree(d_desc);
-        cudaFree(d_counters);
+        dev_free(d_desc);
+        dev_free(d_counters);
     }
 
     // blocks per SM of a stage's kernel (the raster's depends on the scale
@@ -181,8 +181,8 @@ depix_status queue_runner_create(int cap, QueueRunner** out)
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_desc, desc_bytes(cap));
-    if (e == cudaSuccess) e = cudaMalloc(&r->d_counters, QC_COUNT * sizeof(int));
+    if (e == cudaSuccess) e = dev_alloc(&r->d_desc, desc_bytes(cap));
+    if (e == cudaSuccess) e = dev_alloc(&r->d_counters, QC_COUNT * sizeof(int));
     for (int k = 0; k < kSlots && e == cudaSuccess; k++) {
         e = cudaHostAlloc(&r->h_slot[k], desc_bytes(cap), cudaHostAllocDefault);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->slot_copied[k], cudaEventDisableTiming);

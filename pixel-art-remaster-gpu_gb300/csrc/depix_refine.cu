@@ -112,7 +112,7 @@ __device__ __forceinline__ bool reversed_on(int px, int py, int qx, int qy, int 
 
 __device__ __forceinline__ uint32_t cell_word(const Geo& G, int i, int j)
 {
-    return word_of_bgr(load_bgr(G.img, G.ws, G.layout, i, j));
+    return word_of_bgr(load_bgr(G.img, G.ws, G.layout, i, j), G.thr);
 }
 
 // Walks the split edges of cell idx; for each, the twin's owner: the first
@@ -896,16 +896,16 @@ struct DevBuf {
     cudaError_t reserve(size_t n)
     {
         if (n <= cap && p) return cudaSuccess;
-        cudaFree(p);
+        dev_free(p);
         p = nullptr;
         cap = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        cudaError_t e = dev_alloc(&p, std::max<size_t>(n, 1) * sizeof(T));
         if (e == cudaSuccess) cap = n;
         return e;
     }
     void release()
     {
-        cudaFree(p);
+        dev_free(p);
         p = nullptr;
         cap = 0;
     }
@@ -1238,12 +1238,12 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
         RF_CK(r->own_graph.reserve(n));
         RF_CK(r->own_snap.reserve(n));
         const FrameBatch fb{d_img, 0, r->own_snap.p, 0, w, h, widthstep, (int)layout};
-        RF_CK(launch_graph(fb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v), true, s));
+        RF_CK(launch_graph(fb, 1, pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv), true, s));
         RF_CK(launch_heuristics(GraphBatch{r->own_snap.p, r->own_graph.p, 0, w, h, p->vote}, 1, s));
         d_graph = r->own_graph.p;
     }
     Geo G{d_img, widthstep, (int)layout, d_graph, w, h, gw, gh, r->lut, r->box.p,
-          pack_thresholds(p->tr_y, p->tr_u, p->tr_v)};
+          pack_thresholds(p->tr_y, p->tr_u, p->tr_v, p->yuv)};
     RF_CK(r->vgrid.reserve(nv));
     RF_CK(r->cell_count.reserve(n));
     RF_CK(r->cell_off.reserve(n));

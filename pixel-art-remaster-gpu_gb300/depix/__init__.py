@@ -15,6 +15,11 @@ LIB_PATH = os.path.join(PKG, "libdepix.so")
 
 LAYOUT_BGR = 0
 LAYOUT_RGBA = 1
+# depix_status codes
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_ALLOC, ERR_TOO_LARGE, ERR_TIMEOUT, ERR_CAPTURING, ERR_STATE = range(8)
+# luma arithmetic (depix_yuv): the reference's CUDA build, or its host build
+YUV_CUDA = 0
+YUV_HOST = 1
 CELL = 45
 
 
@@ -26,7 +31,8 @@ class DepixError(RuntimeError):
 
 class Params(ctypes.Structure):
     _fields_ = [("tr_y", ctypes.c_int), ("tr_u", ctypes.c_int), ("tr_v", ctypes.c_int),
-                ("subdivide", ctypes.c_int), ("scale", ctypes.c_int), ("vote", ctypes.c_int)]
+                ("subdivide", ctypes.c_int), ("scale", ctypes.c_int), ("vote", ctypes.c_int),
+                ("yuv", ctypes.c_int)]
 
 
 class RefineParams(ctypes.Structure):
@@ -38,11 +44,13 @@ def refine_params(w_curvature=1.0, w_deviation=0.25, w_coverage=1.0, sigma=0.5, 
     return RefineParams(w_curvature, w_deviation, w_coverage, sigma, lr, steps)
 
 
-def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4, vote=False) -> Params:
+def params(tr_y=48, tr_u=7, tr_v=6, subdivide=True, scale=4, vote=False, yuv=YUV_CUDA) -> Params:
     """Frame-path parameters; vote=True resolves ambiguous crossings by the
     weighted vote (curves, sparse pixels, islands) instead of the
-    reference's ordered tests."""
-    return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale, int(bool(vote)))
+    reference's ordered tests; yuv selects the luma arithmetic of the
+    reference's CUDA build (YUV_CUDA, the default) or of its host build
+    (YUV_HOST)."""
+    return Params(tr_y, tr_u, tr_v, int(bool(subdivide)), scale, int(bool(vote)), int(yuv))
 
 
 _lib = None
@@ -69,6 +77,9 @@ def lib():
         _sig(L, "depix_last_error", [], ctypes.c_char_p)
         _sig(L, "depix_init_device", [])
         _sig(L, "depix_take_device_faults", [_vp])
+        _sig(L, "depix_debug_fail_allocations", [_i])
+        _sig(L, "depix_debug_live_allocations", [_vp])
+        _sig(L, "depix_debug_tma_timeout", [_i])
         _sig(L, "depix_graph", [_vp, _i, _i, _i, _i, P, _i, _vp, _vp])
         _sig(L, "depix_resolve_trivial", [_vp, _i, _i, _vp])
         _sig(L, "depix_resolve_heuristics", [_vp, _i, _i, _vp, _vp])
@@ -103,7 +114,7 @@ def lib():
         _sig(L, "depix_refine_energy_grad", [_vp, RP, _vp, _vp, _vp, _vp])
         _sig(L, "depix_refine_warm_start", [_vp, _vp, _vp, _vp, _vp, _vp])
         _sig(L, "depix_refine_run", [_vp, RP, _vp, _vp, _vp, _vp])
-        _sig(L, "depix_yuv_words", [_vp, ctypes.c_size_t, _vp, _vp])
+        _sig(L, "depix_yuv_words", [_vp, ctypes.c_size_t, _i, _vp, _vp])
         _sig(L, "depix_pattern_tables", [_vp, _vp])
         _lib = L
     return _lib
@@ -226,8 +237,8 @@ def raster(img, w, h, ws, layout, g, p, out, stream=None):
            "depix_raster")
 
 
-def yuv_words(px, n, out, stream=None):
-    _check(lib().depix_yuv_words(ptr(px), n, ptr(out), stream_ptr(stream)), "depix_yuv_words")
+def yuv_words(px, n, out, stream=None, yuv=YUV_CUDA):
+    _check(lib().depix_yuv_words(ptr(px), n, int(yuv), ptr(out), stream_ptr(stream)), "depix_yuv_words")
 
 
 def pattern_tables(hull_out, tri_out):
@@ -313,10 +324,33 @@ class Context:
 
 
 def take_device_faults() -> int:
-    """Sticky device-side fault bits since the last call (0: none)."""
+    """Sticky device-side fault bits since the last call (0: none); the C
+    call returns DEPIX_ERR_TIMEOUT (5) whenever a bit is set, which is
+    reported here through the bits, not raised."""
     f = ctypes.c_int(0)
-    _check(lib().depix_take_device_faults(ctypes.byref(f)), "depix_take_device_faults")
+    st = lib().depix_take_device_faults(ctypes.byref(f))
+    if st != ERR_TIMEOUT:
+        _check(st, "depix_take_device_faults")
     return f.value
+
+
+def debug_fail_allocations(after: int) -> None:
+    """Testing hook: after `after` more device allocations by the library
+    succeed, every later one fails until called with a negative value."""
+    _check(lib().depix_debug_fail_allocations(int(after)), "depix_debug_fail_allocations")
+
+
+def debug_live_allocations() -> int:
+    """Testing hook: device allocations the library holds now."""
+    n = ctypes.c_longlong(0)
+    _check(lib().depix_debug_live_allocations(ctypes.byref(n)), "depix_debug_live_allocations")
+    return n.value
+
+
+def debug_tma_timeout(enable: bool) -> None:
+    """Testing hook: the TMA graph kernel issues no tile load and gives up
+    its bounded wait after a few polls (nothing in flight)."""
+    _check(lib().depix_debug_tma_timeout(int(bool(enable))), "depix_debug_tma_timeout")
 
 
 class Refiner:

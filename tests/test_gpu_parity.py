@@ -1,5 +1,7 @@
 """CUDA library (through its C ABI) against the oracle and the reference's
-golden fixtures. Tolerances: the similarity graph, resolved graph, component
+golden fixtures of its host build (frames.npz, yuv.json: luma arithmetic
+DEPIX_YUV_HOST); the CUDA build's fixtures and the CUDA build itself are
+compared in test_gpu_refcuda.py. Tolerances: the similarity graph, resolved graph, component
 labels, cell counts and cell topology are compared bit-exact; vertex
 positions are compared bit-exact too (the pipeline is exact on 1/64-cell
 multiples, far inside the 1e-5 px budget); rasters are compared bit-exact
@@ -45,13 +47,13 @@ def _upload(torch, img, layout):
     return torch.from_numpy(buf.copy()).cuda(), ws
 
 
-def gpu_stages(torch, img, tr, sub, layout, scale=4):
+def gpu_stages(torch, img, tr, sub, layout, scale=4, yuv=0):
     """Runs every stage entry point the way the reference driver chains its kernels."""
     import depix
     h, w = img.shape[:2]
     n = w * h
     d_img, ws = _upload(torch, img, layout)
-    p = depix.params(tr, 7, 6, sub, scale)
+    p = depix.params(tr, 7, 6, sub, scale, yuv=yuv)
     u8 = dict(dtype=torch.uint8, device="cuda")
     raw = torch.empty(n, **u8)
     depix.graph(d_img, w, h, ws, layout, p, raw, fuse_trivial=False)
@@ -83,11 +85,11 @@ def gpu_stages(torch, img, tr, sub, layout, scale=4):
                 raster=c(out).reshape(h * scale, w * scale, 4))
 
 
-def oracle_all(img, tr, sub, scale=4):
+def oracle_all(img, tr, sub, scale=4, yuv=0):
     h, w = img.shape[:2]
     bgr, ws = synth.rgba_to_bgr(img)
-    raw, triv, res = O.graph(bgr, w, h, ws, (tr, 7, 6))
-    f = O.frame(bgr, w, h, ws, sub, (tr, 7, 6))
+    raw, triv, res = O.graph(bgr, w, h, ws, (tr, 7, 6), yuv=yuv)
+    f = O.frame(bgr, w, h, ws, sub, (tr, 7, 6), yuv=yuv)
     assert np.array_equal(f.graph, res)
     return dict(raw=raw, triv=triv, f=f, labels=O.label_cc(res, w, h), raster=O.raster(f.pos, f.col, w, h, scale))
 
@@ -133,14 +135,17 @@ def test_pattern_tables_match_reference(cuda):
             assert (x, y) == tuple(z["points"][k, t]), (k, t)
 
 
-def test_yuv_words_exhaustive(cuda):
+@pytest.mark.parametrize("yuv,fixture", [(1, "yuv.json"), (0, "yuv_cuda.json")])
+def test_yuv_words_exhaustive(cuda, yuv, fixture):
+    """All 2^24 words against the reference's host build (yuv.json) and its
+    CUDA build (yuv_cuda.json)."""
     import depix
     torch = cuda
-    y = json.load(open(os.path.join(GOLDEN, "yuv.json")))
+    y = json.load(open(os.path.join(GOLDEN, fixture)))
     a = torch.arange(1 << 24, dtype=torch.int32, device="cuda")
     px = torch.stack([(a >> 16) & 255, (a >> 8) & 255, a & 255], dim=1).to(torch.uint8).contiguous()
     out = torch.empty(1 << 24, dtype=torch.int32, device="cuda")
-    depix.yuv_words(px, 1 << 24, out)
+    depix.yuv_words(px, 1 << 24, out, yuv=yuv)
     words = out.cpu().numpy().view(np.uint32)
     assert hashlib.sha256(words.astype("<u4").tobytes()).hexdigest() == y["sha256_u32le"]
 
@@ -160,7 +165,7 @@ def test_golden_frames_all_stages(cuda, name, layout):
     img = z[f"{name}/rgba"]
     for tr in (5, 48):
         for sub in (0, 1):
-            g = gpu_stages(cuda, img, tr, sub, layout)
+            g = gpu_stages(cuda, img, tr, sub, layout, yuv=1)
             key = f"{name}/tr{tr}/sub{sub}"
             assert np.array_equal(g["fused"], z[key + "/graph_trivial"])
             assert np.array_equal(g["triv"], z[key + "/graph_trivial"])
@@ -169,7 +174,7 @@ def test_golden_frames_all_stages(cuda, name, layout):
             assert np.array_equal(_defined_hull(g["hull"], g["ec_cells"]), z[key + "/hull"])
             assert np.array_equal(g["ec"], z[key + "/ec"])
             assert np.array_equal(_defined_pos(g["pos"], g["ec"]), z[key + "/pos"])
-            compare(g, oracle_all(img, tr, sub))
+            compare(g, oracle_all(img, tr, sub, yuv=1))
 
 
 @pytest.mark.parametrize("name", ["c_pattern", "alex"])

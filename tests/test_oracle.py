@@ -1,6 +1,8 @@
 """The CPU oracle against the reference: committed golden fixtures made by the
-reference's own stage bodies, its known-answer graph dumps and border walks,
-and (when built in this checkout) the reference's host build directly."""
+reference's own stage bodies in both of its builds (host: frames.npz,
+yuv.json, luma arithmetic YUV_HOST; CUDA: frames_cuda.npz, yuv_cuda.json,
+YUV_CUDA), its known-answer graph dumps and border walks, and (when built in
+this checkout) the reference's host build directly."""
 import hashlib
 import json
 import os
@@ -48,7 +50,7 @@ def test_oracle_matches_reference_golden(frames, name, tr, sub):
     img = frames[f"{name}/rgba"]
     h, w = img.shape[:2]
     bgr, ws = synth.rgba_to_bgr(img)
-    f = O.frame(bgr, w, h, ws, sub, (tr, 7, 6))
+    f = O.frame(bgr, w, h, ws, sub, (tr, 7, 6), yuv=O.YUV_HOST)
     key = f"{name}/tr{tr}/sub{sub}"
     assert np.array_equal(f.graph_trivial, frames[key + "/graph_trivial"])
     assert np.array_equal(f.graph, frames[key + "/graph"])
@@ -91,13 +93,73 @@ def test_component_labels_contain_reference_border_walks():
     assert all(lab[k] <= k and lab[lab[k]] == lab[k] for k in range(576))
 
 
+def _all_colours():
+    allc = np.stack(np.meshgrid(np.arange(256), np.arange(256), np.arange(256), indexing="ij"), -1)
+    return allc.reshape(-1, 3).astype(np.uint8)
+
+
 def test_yuv_words_exhaustive_against_reference():
     y = json.load(open(os.path.join(GOLDEN, "yuv.json")))
-    allc = np.stack(np.meshgrid(np.arange(256), np.arange(256), np.arange(256), indexing="ij"), -1)
-    allc = allc.reshape(-1, 3).astype(np.uint8)
-    words = O.yuv_words(allc)
+    words = O.yuv_words(_all_colours(), yuv=O.YUV_HOST)
     assert hashlib.sha256(words.astype("<u4").tobytes()).hexdigest() == y["sha256_u32le"]
     assert words[np.array(y["sample_index"])].tolist() == y["sample_word"]
+
+
+def test_yuv_words_exhaustive_against_reference_cuda_build():
+    """The luma of the CUDA build: the oracle's fused multiply-add order gives
+    the CUDA build's word for all 2^24 colours, and differs from the host
+    build exactly on the colours the fixture lists."""
+    y = json.load(open(os.path.join(GOLDEN, "yuv_cuda.json")))
+    allc = _all_colours()
+    words = O.yuv_words(allc, yuv=O.YUV_CUDA)
+    assert hashlib.sha256(words.astype("<u4").tobytes()).hexdigest() == y["sha256_u32le"]
+    host = O.yuv_words(allc, yuv=O.YUV_HOST)
+    assert np.nonzero(words != host)[0].tolist() == y["differs_from_host_build"]
+    assert len(y["differs_from_host_build"]) == 2490
+    # every such colour has an exact integer sum 0.299 r + 0.587 g + 0.114 b
+    d = np.array(y["differs_from_host_build"])
+    r, g, b = allc[d, 0].astype(np.int64), allc[d, 1].astype(np.int64), allc[d, 2].astype(np.int64)
+    assert ((299 * r + 587 * g + 114 * b) % 1000 == 0).all()
+
+
+def _cuda_golden_runs():
+    z = np.load(os.path.join(GOLDEN, "frames_cuda.npz"))
+    for name in sorted({k.split("/")[0] for k in z.files}):
+        for tr in (5, 48):
+            for sub in (0, 1):
+                yield name, tr, sub
+
+
+@pytest.fixture(scope="module")
+def frames_cuda():
+    return np.load(os.path.join(GOLDEN, "frames_cuda.npz"))
+
+
+@pytest.mark.parametrize("name,tr,sub", list(_cuda_golden_runs()))
+def test_oracle_matches_reference_cuda_build_golden(frames_cuda, name, tr, sub):
+    z = frames_cuda
+    img = z[f"{name}/rgba"]
+    h, w = img.shape[:2]
+    bgr, ws = synth.rgba_to_bgr(img)
+    f = O.frame(bgr, w, h, ws, sub, (tr, 7, 6), yuv=O.YUV_CUDA)
+    key = f"{name}/tr{tr}/sub{sub}"
+    assert np.array_equal(f.graph_trivial, z[key + "/graph_trivial"])
+    assert np.array_equal(f.graph, z[key + "/graph"])
+    assert np.array_equal(f.ec_cells, z[key + "/ec_cells"])
+    assert np.array_equal(_defined_hull(f.diag_cells, f.ec_cells), z[key + "/hull"])
+    assert np.array_equal(f.ec, z[key + "/ec"])
+    assert np.array_equal(_defined_pos(f.pos, f.ec), z[key + "/pos"])
+
+
+def test_the_two_builds_differ_on_grey_frames(frames_cuda):
+    """The fixtures of the two builds are not the same data: on the grey
+    frames the CUDA build's graphs differ from the host build's."""
+    z = frames_cuda
+    img = z["grey_k/rgba"]
+    h, w = img.shape[:2]
+    bgr, ws = synth.rgba_to_bgr(img)
+    host = O.frame(bgr, w, h, ws, 0, (5, 7, 6), yuv=O.YUV_HOST)
+    assert not np.array_equal(host.graph_trivial, z["grey_k/tr5/sub0/graph_trivial"])
 
 
 def _bfs_labels(g, w, h):
@@ -172,7 +234,7 @@ def test_oracle_equals_reference_build_full_frames(seed, tr):
         h, w = img.shape[:2]
         bgr, ws = synth.rgba_to_bgr(img)
         for sub in (0, 1):
-            a = O.frame(bgr, w, h, ws, sub, (tr, 7, 6))
+            a = O.frame(bgr, w, h, ws, sub, (tr, 7, 6), yuv=O.YUV_HOST)
             b = O.ref_frame(bgr, w, h, ws, sub, tr)
             assert np.array_equal(a.graph_trivial, b.graph_trivial)
             assert np.array_equal(a.graph, b.graph)

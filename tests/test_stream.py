@@ -23,7 +23,7 @@ class OracleContext:
         for k, (w, h) in enumerate(zip(ws.tolist(), hs.tolist())):
             img = h_img[int(in_off[k]):int(in_off[k]) + w * h * 4].reshape(h, w, 4)
             bgr, wstep = synth.rgba_to_bgr(img)
-            f = O.frame(bgr, w, h, wstep, p.subdivide, (p.tr_y, p.tr_u, p.tr_v))
+            f = O.frame(bgr, w, h, wstep, p.subdivide, (p.tr_y, p.tr_u, p.tr_v), yuv=p.yuv)
             r = O.raster(f.pos, f.col, w, h, s).reshape(-1)
             assert int(out_off[k]) + r.size <= out_bytes
             h_out[int(out_off[k]):int(out_off[k]) + r.size] = r
@@ -33,7 +33,7 @@ class OracleContext:
 
 
 class Params:
-    tr_y, tr_u, tr_v, subdivide, scale = 48, 7, 6, 1, 2
+    tr_y, tr_u, tr_v, subdivide, scale, yuv = 48, 7, 6, 1, 2, 0
 
 
 def _expected(img, s):
