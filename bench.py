@@ -438,7 +438,7 @@ def run_latency(args, dev, stream, ctx, frames, B_max):
     out["plain"]["frames"] = n_frames
     rows = []
     for b in (8, 32, 128, 1024):
-        if b > ctx.max_frames:
+        if b > B_max:
             continue
         ws_b, hs_b = np.full(b, W, np.int32), np.full(b, H, np.int32)
         io = np.arange(b, dtype=np.uint64) * np.uint64(in_bytes)

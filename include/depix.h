@@ -231,7 +231,10 @@ depix_status depix_pattern_tables(uint64_t* h_hull, uint64_t* h_tri);
  *  - every device that loads the library holds the 4 MiB array until the
  *    process exits;
  *  - the first call on a device looks up the array's device address (no
- *    allocation); make that first call before capturing any stream;
+ *    allocation); make that first call before capturing any stream. The
+ *    address is kept per device and looked up again when the calling
+ *    thread's current context is not the one it was found in (after
+ *    cudaDeviceReset);
  *  - all calls share the one array: calls whose work overlaps on the GPU
  *    (different streams, no ordering between them) race on it. */
 #define DEPIX_STATIC_MAX_PIXELS 4194304

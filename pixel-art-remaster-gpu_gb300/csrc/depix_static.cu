@@ -21,10 +21,35 @@ constexpr size_t kStaticSnapshotBytes = (size_t)DEPIX_STATIC_MAX_PIXELS; // one 
 static __device__ __align__(256) uint8_t g_static_snapshot[kStaticSnapshotBytes];
 
 std::mutex g_static_mu;
-std::vector<uint8_t*> g_static_addr; // device address of g_static_snapshot, per device
+struct StaticAddr {
+    uint8_t* p = nullptr; // device address of g_static_snapshot
+    CUcontext ctx = nullptr; // the context it was looked up in
+};
+std::vector<StaticAddr> g_static_addr; // per device
 
-// Looks up the array's device address once per device, with that device
-// current. The host-side name g_static_snapshot is not a device address.
+// The calling thread's current context (driver entry point reached through
+// the runtime; nullptr when unavailable).
+CUcontext current_context()
+{
+    using GetCurrent = CUresult (*)(CUcontext*);
+    static GetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<GetCurrent>(p);
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// Looks up the array's device address once per device and context, with
+// that device current. The host-side name g_static_snapshot is not a device
+// address. A saved address is reused only in the context it was looked up
+// in: after cudaDeviceReset the device's primary context is a new one, and
+// the array's address is looked up again.
 depix_status static_snapshot(uint8_t** out)
 {
     int dev = 0;
@@ -34,8 +59,9 @@ depix_status static_snapshot(uint8_t** out)
         return DEPIX_ERR_CUDA;
     }
     std::lock_guard<std::mutex> lk(g_static_mu);
-    if (dev < (int)g_static_addr.size() && g_static_addr[dev]) {
-        *out = g_static_addr[dev];
+    CUcontext ctx = current_context();
+    if (dev < (int)g_static_addr.size() && g_static_addr[dev].p && ctx && g_static_addr[dev].ctx == ctx) {
+        *out = g_static_addr[dev].p;
         return DEPIX_OK;
     }
     void* p = nullptr;
@@ -44,9 +70,11 @@ depix_status static_snapshot(uint8_t** out)
         depix::set_last_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         return DEPIX_ERR_CUDA;
     }
-    if (dev >= (int)g_static_addr.size()) g_static_addr.resize(dev + 1, nullptr);
-    g_static_addr[dev] = static_cast<uint8_t*>(p);
-    *out = g_static_addr[dev];
+    if (dev >= (int)g_static_addr.size()) g_static_addr.resize(dev + 1);
+    // the first call in a context made that context current (cudaGetDevice
+    // and the lookup above), so ctx is set from then on
+    g_static_addr[dev] = StaticAddr{static_cast<uint8_t*>(p), ctx ? ctx : current_context()};
+    *out = g_static_addr[dev].p;
     return DEPIX_OK;
 }
 

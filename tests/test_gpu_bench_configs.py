@@ -1,0 +1,77 @@
+"""The benchmarked configurations themselves against the oracle, frame by
+frame, through the same calls the benchmark times:
+  - the uniform batch of 256x224 RGBA8 frames (seeded benchmark generator),
+    x4, subdivision, component labels and the default crossing decision
+    (the reference's ordered tests), 16 distinct frames through depix_batch:
+    the grid kernels of the headline leg (TMA graph, heuristics with fused
+    local labels, label merge and flatten, TMA raster);
+  - the full 4096-sprite uneven batch (sides ~ U[8, 64], 30 % transparent
+    backgrounds), x4 with labels, through the tuned persistent tile-queue
+    path, every sprite.
+Rasters bit-exact (budget: 1 LSB on 0.1 % of pixels), labels bit-exact."""
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+import oracle as O
+from depix import synth
+
+from test_gpu_parity import assert_raster_close
+from test_gpu_queue import _pack
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(img, scale=4):
+    h, w = img.shape[:2]
+    bgr, ws = synth.rgba_to_bgr(img)
+    f = O.frame(bgr, w, h, ws, 1, (48, 7, 6))
+    return O.raster(f.pos, f.col, w, h, scale), O.label_cc(f.graph, w, h)
+
+
+def _check_all(imgs, rasters, labels):
+    with ThreadPoolExecutor(max_workers=16) as ex:  # the oracle's C calls release the GIL
+        want = list(ex.map(_oracle, imgs))
+    for k, (wr, wl) in enumerate(want):
+        assert_raster_close(rasters[k], wr)
+        assert np.array_equal(labels[k], wl), f"frame {k}: labels differ"
+
+
+def _run_batch(torch, imgs, scale=4):
+    import depix
+    buf, in_off, out_off, out_bytes = _pack(imgs, scale)
+    d_in = torch.from_numpy(buf).cuda()
+    d_out = torch.full((out_bytes,), 7, dtype=torch.uint8, device="cuda")
+    npx = sum(i.shape[0] * i.shape[1] for i in imgs)
+    d_lab = torch.full((npx,), -5, dtype=torch.int32, device="cuda")
+    ctx = depix.Context(max(i.shape[0] * i.shape[1] for i in imgs), len(imgs))
+    ws = np.array([i.shape[1] for i in imgs], np.int32)
+    hs = np.array([i.shape[0] for i in imgs], np.int32)
+    ctx.batch(ws, hs, np.array(in_off, np.uint64), np.array(out_off, np.uint64), d_in, depix.params(scale=scale),
+              d_out, d_lab)
+    torch.cuda.synchronize()
+    assert depix.take_device_faults() == 0
+    shape = ctx.launch_shape()
+    ctx.close()
+    out, lab = d_out.cpu().numpy(), d_lab.cpu().numpy()
+    rasters, labels, o = [], [], 0
+    for k, img in enumerate(imgs):
+        h, w = img.shape[:2]
+        rasters.append(out[out_off[k]:out_off[k] + w * h * 4 * scale * scale].reshape(h * scale, w * scale, 4))
+        labels.append(lab[o:o + w * h])
+        o += w * h
+    return rasters, labels, shape
+
+
+def test_uniform_256x224_batch_with_labels_default_decision(cuda):
+    imgs = [np.ascontiguousarray(synth.frame(seed)) for seed in range(16)]
+    rasters, labels, _ = _run_batch(cuda, imgs)
+    _check_all(imgs, rasters, labels)
+
+
+def test_4096_sprite_batch_every_sprite(cuda):
+    imgs = [np.ascontiguousarray(i) for i in synth.sprites(4096, seed=0)]
+    assert len(imgs) == 4096
+    rasters, labels, shape = _run_batch(cuda, imgs)
+    _check_all(imgs, rasters, labels)

@@ -134,6 +134,31 @@ def test_adjoint_matches_central_differences(small):
     assert np.linalg.norm(g[sel] - fd) <= GRAD_RTOL * np.linalg.norm(fd)
 
 
+def test_adjoint_on_the_256x224_frame(cuda):
+    """The check of the workload's own frame (256x224, seed 0, x4): the
+    adjoint at perturbed positions against the float64 analytic gradient on
+    every node, and against float64 central differences (h = 1e-4) on 256
+    random free nodes, each difference formed from the energy terms that
+    touch its node (the rest cancel exactly)."""
+    torch = cuda
+    img = synth.frame(0)
+    rf, rp, raw, res = _setup(torch, img)
+    top = R.topology(img, res, raw, 4)
+    d_pos, P, P0 = _perturbed(torch, top, rf, seed=11)
+    d_grad = torch.zeros_like(d_pos)
+    e = rf.energy_grad(rp, d_pos, d_grad)
+    parts, total, G = R.energy_grad(top, P, P0, img)
+    assert abs(e[3] - total) <= ENERGY_RTOL * total
+    g = d_grad.cpu().numpy().reshape(-1, 2).astype(np.float64)
+    assert np.linalg.norm(g - G) <= GRAD_RTOL * np.linalg.norm(G)
+    free = np.nonzero(top.free)[0]
+    sel = np.random.default_rng(5).choice(free, 256, replace=False)
+    fd = R.central_differences_local(top, P, P0, img, sel, h=1e-4)
+    assert np.linalg.norm(g[sel] - fd) <= GRAD_RTOL * np.linalg.norm(fd)
+    assert np.linalg.norm(G[sel] - fd) <= 1e-6 * np.linalg.norm(fd)
+    rf.close()
+
+
 def test_adam_on_the_gpu_follows_float64_adam(small):
     """One step moves every node whose gradient is clear of float32 noise by
     the same amount as float64 Adam (the first Adam step is lr * g / (|g| +

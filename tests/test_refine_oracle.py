@@ -39,6 +39,21 @@ def test_gradient_matches_central_differences(small):
     assert np.all(G[~top.free] == 0)
 
 
+def test_local_central_differences_equal_full_ones(small):
+    """The per-node differences from only the terms touching the node equal
+    the differences of the whole energy (the other terms cancel)."""
+    img, top = small
+    P0 = R.initial_positions(top)
+    rng = np.random.default_rng(2)
+    free = np.nonzero(top.free)[0]
+    P = P0.copy()
+    P[free] += rng.normal(0, 0.05, (len(free), 2))
+    sel = np.concatenate([rng.choice(free, 24, replace=False), np.nonzero(~top.free)[0][:4]])
+    full = R.central_differences(top, P, P0, img, sel, h=1e-4)
+    local = R.central_differences_local(top, P, P0, img, sel, h=1e-4)
+    assert np.abs(full - local).max() <= 1e-9 * max(np.abs(full).max(), 1e-12) + 1e-11
+
+
 def test_topology_invariants(small):
     img, top = small
     assert len(top.qx) > 100 and top.free.sum() > 50

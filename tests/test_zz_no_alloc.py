@@ -2,7 +2,8 @@
 snapshot lives in a fixed device array inside the library, for callers that
 cannot allocate device memory. Called through the C ABI and compared, bit for
 bit, with depix_resolve_heuristics (which takes the snapshot from the caller)
-on two calls in a row. This file is collected last on purpose."""
+on consecutive calls. This file is collected last on purpose, after
+test_zz_device_faults.py."""
 import ctypes
 
 import numpy as np
@@ -26,9 +27,11 @@ def test_static_snapshot_equals_caller_snapshot_on_consecutive_calls(cuda):
     torch = cuda
     fn = _entry(depix)
     p = depix.params()
-    # two calls in a row, the second on a smaller frame: whatever the first
-    # left in the shared array must not leak into the second
-    for img in (synth.frame_large(5, w=320, h=240), synth.frame(31)):
+    # calls in a row, each on a smaller frame: whatever the previous call
+    # left in the shared array must not leak into the next; the last frame's
+    # width is not a multiple of 16, so the heuristics read the array with
+    # plain loads instead of a TMA tile load
+    for img in (synth.frame_large(5, w=320, h=240), synth.frame(31), synth.frame(7, w=250, h=97)):
         h, w = img.shape[:2]
         d_img = torch.from_numpy(np.ascontiguousarray(img).reshape(-1).copy()).cuda()
         after_trivial = torch.empty(w * h, dtype=torch.uint8, device="cuda")
@@ -42,6 +45,8 @@ def test_static_snapshot_equals_caller_snapshot_on_consecutive_calls(cuda):
         assert torch.equal(in_place, expected)
         bgr, ws = synth.rgba_to_bgr(img)
         assert np.array_equal(in_place.cpu().numpy(), O.graph(bgr, w, h, ws)[2])
+    # no bounded wait of the TMA tile loads (which read the array) gave up
+    assert depix.take_device_faults() == 0
 
 
 def test_static_snapshot_rejects_frames_beyond_its_size(cuda):
