@@ -305,6 +305,29 @@ def run_ours(args, rank, world, local_rank):
     # stream, over back-to-back calls; frames/s over the same calls
     latency = run_latency(args, dev, stream, ctx, frames, B)
 
+    # plain per-frame path, device-resident input: one launch per stage and frame
+    pf = max(args.plain_frames, 10)
+    ctx1 = depix.Context(W * H, 1)
+    lat = []
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(pf)]
+    for k in range(5):
+        ctx1.frame(d_in[k * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out, None, d_lab, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(pf):
+        a, b = evs[k]
+        a.record(stream)
+        f = k % B
+        ctx1.frame(d_in[f * in_bytes:], W, H, 4 * W, depix.LAYOUT_RGBA, p, d_out[f * out_px * 4:], None,
+                   d_lab[f * W * H:], stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    lat = sorted(a.elapsed_time(b) for a, b in evs)
+    plain = {"frames_per_s": round(pf / plain_s, 1), "p50_ms_per_frame": round(lat[len(lat) // 2], 4),
+             "p99_ms_per_frame": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4), "frames": pf}
+    ctx1.close()
+
     # the same batch with the weighted-vote heuristics (depix_params.vote)
     vote = None
     if not args.no_vote:
