@@ -681,28 +681,26 @@ __device__ __forceinline__ unsigned spill_bits(int x0, int y0, int x1, int y1)
 // points and, on a linked/border transition, the linked neighbour's R (or Q)
 // around the vertex matching this one (getPointIndex falls back to vertex 0).
 // NbPattern(L) is the pattern of the neighbour in direction L; TJ(px, py) the
-// corner test of a vertex between two border edges.
-template <typename NbPattern, typename TJ>
-__device__ __forceinline__ void subdivide_tables(int pat, uint64_t e, NbPattern nb_pattern, TJ tj, Packed& out)
+// corner test of a vertex between two border edges; Emit(t, x, y) receives
+// cut vertex t. Returns the vertex count.
+template <typename NbPattern, typename TJ, typename Emit>
+__device__ __forceinline__ int subdivide_tables(int pat, uint64_t e, NbPattern nb_pattern, TJ tj, Emit emit)
 {
     const int n = (int)(e & 0xF);
     const uint64_t vk = __ldg(&g_vk_lut[pat]);
-    const uint4* qrv = reinterpret_cast<const uint4*>(g_qr_lut + pat * 8);
-    const uint4 qa = __ldg(qrv), qb = __ldg(qrv + 1);
-    out.x0 = out.x1 = out.y0 = out.y1 = 0;
+    const uint32_t* qrs = g_qr_lut + pat * 8;
     int m = 0;
     for (int v = 0; v < n; v++) {
         const int code = (int)((vk >> (5 * v)) & 31u), kind = code & 3;
         const int px = hx(e, v), py = hy(e, v);
-        const uint32_t qr = v < 4 ? (v < 2 ? (v == 0 ? qa.x : qa.y) : (v == 2 ? qa.z : qa.w))
-                                  : (v < 6 ? (v == 4 ? qb.x : qb.y) : (v == 6 ? qb.z : qb.w));
+        const uint32_t qr = __ldg(qrs + v);
         const int qx = (int8_t)(qr & 0xFF), qy = (int8_t)((qr >> 8) & 0xFF);
         const int rx = (int8_t)((qr >> 16) & 0xFF), ry = (int8_t)(qr >> 24);
         if (kind == 0 || (kind == 1 && tj(px, py))) {
-            pk_put(out, m++, px, py);
+            emit(m++, px, py);
         } else if (kind == 1) {
-            pk_put(out, m++, rx, ry);
-            pk_put(out, m++, qx, qy);
+            emit(m++, rx, ry);
+            emit(m++, qx, qy);
         } else {
             const int L = code >> 2, ddx = dir_di(L), ddy = dir_dj(L);
             const int np = nb_pattern(L);
@@ -731,15 +729,15 @@ __device__ __forceinline__ void subdivide_tables(int pat, uint64_t e, NbPattern 
             ax += kUnit * ddx;
             ay += kUnit * ddy;
             if (kind == 2) {
-                pk_put(out, m++, (qx + ax) / 2, (qy + ay) / 2);
-                pk_put(out, m++, qx, qy);
+                emit(m++, (qx + ax) / 2, (qy + ay) / 2);
+                emit(m++, qx, qy);
             } else {
-                pk_put(out, m++, rx, ry);
-                pk_put(out, m++, (rx + ax) / 2, (ry + ay) / 2);
+                emit(m++, rx, ry);
+                emit(m++, (rx + ax) / 2, (ry + ay) / 2);
             }
         }
     }
-    out.n = m;
+    return m;
 }
 
 // Coverage of a polygon that is not star-shaped around its cell centre: the
@@ -762,8 +760,8 @@ __device__ __noinline__ int ear_clip_mask(const Packed& P, int u, int mlo, int F
 // The cut polygon of a subdivided cell (G(dx, dy): graph byte of the cell at
 // that offset, 0 outside the image, bits toward outside cleared; TJ(px, py):
 // the corner test).
-template <typename GraphAt, typename TJ>
-__device__ __forceinline__ void cell_polygon(GraphAt G, TJ tj, Packed& sp)
+template <typename GraphAt, typename TJ, typename Emit>
+__device__ __forceinline__ int cell_polygon_emit(GraphAt G, TJ tj, Emit emit)
 {
     const unsigned node = G(0, 0);
     const int pat = cell_pattern(node, G(-1, 0), G(1, 0));
@@ -772,7 +770,31 @@ __device__ __forceinline__ void cell_polygon(GraphAt G, TJ tj, Packed& sp)
         const int dx = dir_di(L), dy = dir_dj(L);
         return cell_pattern(G(dx, dy), G(dx - 1, dy), G(dx + 1, dy));
     };
-    subdivide_tables(pat, e, nb_pattern, tj, sp);
+    return subdivide_tables(pat, e, nb_pattern, tj, emit);
+}
+
+// The cut polygon in registers.
+template <typename GraphAt, typename TJ>
+__device__ __forceinline__ void cell_polygon(GraphAt G, TJ tj, Packed& sp)
+{
+    sp.x0 = sp.x1 = sp.y0 = sp.y1 = 0;
+    sp.n = cell_polygon_emit(G, tj, [&](int t, int x, int y) { pk_put(sp, t, x, y); });
+}
+
+// The cut polygon written straight into 9 parked words (rows[0..3] the x
+// bytes, rows[4..7] the y bytes, rows[8] the count: park_polygon's layout),
+// one byte store per coordinate.
+template <typename GraphAt, typename TJ>
+__device__ __forceinline__ void cell_polygon_parked(GraphAt G, TJ tj, uint32_t* rows)
+{
+#pragma unroll
+    for (int r = 0; r < 8; r++) rows[r] = 0u;
+    uint8_t* xb = reinterpret_cast<uint8_t*>(rows);
+    uint8_t* yb = xb + 16;
+    rows[8] = (uint32_t)cell_polygon_emit(G, tj, [&](int t, int x, int y) {
+        xb[t] = (uint8_t)x;
+        yb[t] = (uint8_t)y;
+    });
 }
 
 // Coverage rows of a cut polygon and its spill bits (0 when the ear clip
@@ -791,17 +813,10 @@ __device__ __forceinline__ unsigned polygon_mask(const Packed& sp, const MaskGeo
     return spill_bits(mnx, mny, mxx, mxy);
 }
 
-// A cut polygon parked in its own cell's mask rows (10 words) until the mask
-// is made, and a 64-bit mix of it for the tile's table of distinct polygons.
-__device__ __forceinline__ void park_polygon(const Packed& sp, uint32_t* rows)
-{
-    rows[0] = (uint32_t)sp.x0; rows[1] = (uint32_t)(sp.x0 >> 32);
-    rows[2] = (uint32_t)sp.x1; rows[3] = (uint32_t)(sp.x1 >> 32);
-    rows[4] = (uint32_t)sp.y0; rows[5] = (uint32_t)(sp.y0 >> 32);
-    rows[6] = (uint32_t)sp.y1; rows[7] = (uint32_t)(sp.y1 >> 32);
-    rows[8] = (uint32_t)sp.n;
-}
-
+// A cut polygon parked in its own cell's mask rows until the mask is made
+// (rows[0..3] the x bytes, rows[4..7] the y bytes, rows[8] the count, as
+// cell_polygon_parked writes it), and a 64-bit mix of it for the tile's table
+// of distinct polygons.
 __device__ __forceinline__ void unpark_polygon(const uint32_t* rows, Packed& sp)
 {
     sp.x0 = rows[0] | (uint64_t)rows[1] << 32;
@@ -1036,9 +1051,9 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
             const int bx = lx + 2, by = ly + 2;
             auto Gs = [&](int dx, int dy) -> unsigned { return M.graph[by + dy][bx + dx + T::kGOff]; };
             auto tj = [&](int px, int py) -> bool { return tj_of(lx, ly, ci, cj, border, px, py); };
+            cell_polygon_parked(Gs, tj, masks + (size_t)k * F);
             Packed sp;
-            cell_polygon(Gs, tj, sp);
-            park_polygon(sp, masks + (size_t)k * F);
+            unpark_polygon(masks + (size_t)k * F, sp);
             __threadfence_block();
             const int rp = dedupe(polygon_hash(sp), 1, q, [&](int rq) {
                 Packed o;
