@@ -1150,8 +1150,7 @@ __device__ void mask_raster_tile(MaskTile<TW, TH>& M, uint32_t* masks, const uin
                 for (int di = 1; di >= -1; di--, qq++) {
                     take[qq] = 0;
                     if (rr < 0 || rr >= F) continue;
-                    const int kn = k0 + dj * T::GW + di;
-                    if (!M.live[kn]) continue;
+                    const int kn = k0 + dj * T::GW + di; // cells outside the image have zero rows
                     const uint64_t wbits = masks[(size_t)kn * F + rr];
                     const int sh = s * di + G.mlo; // block column c = footprint column + sh
                     const uint32_t bits =
