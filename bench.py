@@ -810,7 +810,7 @@ def run_stream(args, dev, stream):
         side[k].wait_event(uploaded)
         rf.setup(d_in[k * fb:], W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp, stream=side[k])
         assert rf.counts()["nodes"] <= cap
-        done = torch.cuda.Event()
+        done = torch.cuda.Event(enable_timing=True)
         done.record(side[k])
         return done
 
@@ -824,11 +824,17 @@ def run_stream(args, dev, stream):
             uploaded = torch.cuda.Event()
             uploaded.record(stream)
             ctx.batch([W] * B, [H] * B, in_off, out_off, d_in, p, d_out, None, stream=stream)
+            rastered = ev()
+            rastered.record(stream)
             cur = rfs[bi % 2]
             futs = [pool.submit(setup, cur[k], k, uploaded) for k in range(B)]
+            marks = (start, rastered, [], [])
+            batch_marks.append(marks)
             for k in range(B):
                 rf, ps = cur[k], pos[bi % 2][k]
-                stream.wait_event(futs[k].result())
+                set_up = futs[k].result()
+                marks[2].append(set_up)
+                stream.wait_event(set_up)
                 if prev is None:
                     rf.initial(ps, stream=stream)
                 else:
@@ -840,20 +846,31 @@ def run_stream(args, dev, stream):
                 done = ev()
                 done.record(stream)
                 lat_marks.append((start, done))
+                marks[3].append(done)
                 prev = (rf, ps)
             # the next batch's upload is ordered after these steps on the main
             # stream, and its setups (the other refiner set) wait for that upload
         return reused, tiles
 
-    lat_marks = []
+    lat_marks, batch_marks = [], []
     run_all(False)  # warm-up pass
     torch.cuda.synchronize()
-    lat_marks = []
+    lat_marks, batch_marks = [], []
     t0 = time.perf_counter()
     run_all(False)
     torch.cuda.synchronize()
     batched_s = time.perf_counter() - t0
     lat = sorted(a.elapsed_time(b) for a, b in lat_marks)
+    # where a batch's time goes: upload + batch raster, the eight topology
+    # setups (concurrent, each with host readbacks of its counts), then warm
+    # start + Adam steps frame after frame
+    med = lambda v: round(float(np.median(v)), 4)
+    breakdown = {
+        "upload_raster_ms": med([m[0].elapsed_time(m[1]) for m in batch_marks]),
+        "setups_done_ms": med([max(m[0].elapsed_time(e) for e in m[2]) for m in batch_marks]),
+        "first_frame_done_ms": med([m[0].elapsed_time(m[3][0]) for m in batch_marks]),
+        "refine_per_frame_ms": med([(m[3][0].elapsed_time(m[3][-1])) / (B - 1) for m in batch_marks]),
+    }
     lat_marks = []
     reused, tiles = run_all(True)
     torch.cuda.synchronize()
@@ -862,8 +879,10 @@ def run_stream(args, dev, stream):
     rfs = [rfs_flat[0], rfs_flat[1]]
     pos = [pos[0][0], pos[0][1]]
 
-    # warm against cold start: energy after 20 steps on a few frames
-    warm_e, cold_e = [], []
+    # warm against cold start: energy after 20 steps on a few frames, and the
+    # cold-start steps that reach the warm start's 20-step energy
+    warm_e, cold_e, cold_steps = [], [], []
+    ladder = [20, 25, 30, 40, 50, 60, 80, 100, 150, 200]
     for f in range(1, 17):
         rf, ps = rfs[f % 2], pos[f % 2]
         prv = rfs[(f - 1) % 2]
@@ -877,6 +896,12 @@ def run_stream(args, dev, stream):
         rf.warm_start(prv, pp, ps, stream=stream, count=False)
         warm_e.append(rf.run(rp, ps, stream=stream)[1][3])
         cold_e.append(rf.run(rp, None, stream=stream)[1][3])
+        need = None
+        for k in ladder:
+            if rf.run(depix.refine_params(steps=k), None, stream=stream)[1][3] <= warm_e[-1]:
+                need = k
+                break
+        cold_steps.append(need if need is not None else 10 ** 9)
     for r in rfs_flat:
         r.close()
     ctx.close()
@@ -888,7 +913,12 @@ def run_stream(args, dev, stream):
             "batched_refined": {"frames_per_s": round(n / batched_s, 1), "p50_ms": pct(lat, 0.5),
                                 "p99_ms": pct(lat, 0.99), "batch": B, "reused_tile_frac": round(reused / max(tiles, 1), 4)},
             "energy_after_20_steps": {"warm_start": round(float(np.mean(warm_e)), 6),
-                                      "cold_start": round(float(np.mean(cold_e)), 6), "frames": len(warm_e)}}
+                                      "cold_start": round(float(np.mean(cold_e)), 6), "frames": len(warm_e),
+                                      "cold_steps_to_warm_energy_median": int(np.median(cold_steps)),
+                                      "cold_steps_to_warm_energy": [int(c) if c < 10 ** 9 else None
+                                                                    for c in cold_steps],
+                                      "ladder": ladder},
+            "batch_breakdown": breakdown}
 
 
 # ---------------------------------------------------------- reference arm
