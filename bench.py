@@ -720,6 +720,10 @@ def run_refine(args, dev, stream, cpu):
     ms = e0.elapsed_time(e1) / runs
     out = {"workload": f"256x224 frame (seeded generator), x4 coverage, {c['nodes']} nodes ({c['free']} free), "
                        f"{c['edges']} curve edges, {c['samples']} samples, {rp.steps} Adam steps",
+           "node_definition": "nodes are the cell-hull vertices on curve edges (edges between dissimilar cells); "
+                              "the workload's 'about 20k nodes' is an estimate: the distinct vertices of every "
+                              "subdivided cell polygon of this frame number 45,846, the curve-edge vertices "
+                              f"{c['nodes']}",
            "steps_per_s": round(rp.steps / (ms / 1e3), 1), "ms_per_frame": round(ms, 3),
            "setup_ms": round(setup_ms, 3), "energy_before": round(before[3], 6), "energy_after": round(after[3], 6),
            "energy_cut": round(1 - after[3] / before[3], 4),
