@@ -162,18 +162,6 @@ def test_the_two_builds_differ_on_grey_frames(frames_cuda):
     assert not np.array_equal(host.graph_trivial, z["grey_k/tr5/sub0/graph_trivial"])
 
 
-def test_integer_chroma_equals_the_float_products():
-    """The library computes u = int((b - y) * 0.492f) and v = int((r - y) *
-    0.877f) as truncated integer quotients; for every difference the luma
-    allows they equal the float products of both reference builds."""
-    d = np.arange(-255, 256, dtype=np.int64)
-    uf = (d.astype(np.float32) * np.float32(0.492)).astype(np.int64)
-    vf = (d.astype(np.float32) * np.float32(0.877)).astype(np.int64)
-    ui = np.sign(d) * (np.abs(d) * 492 // 1000)
-    vi = np.sign(d) * (np.abs(d) * 877 // 1000)
-    assert np.array_equal(uf, ui) and np.array_equal(vf, vi)
-
-
 def _bfs_labels(g, w, h):
     di = [-1, 0, 1, -1, 1, -1, 0, 1]
     dj = [1, 1, 1, 0, 0, -1, -1, -1]
