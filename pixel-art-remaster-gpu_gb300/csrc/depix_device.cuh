@@ -849,6 +849,22 @@ __device__ __forceinline__ void queue_loop(int* counter, int total, int gran, Bo
     }
 }
 
+// The same with each warp pulling its own tiles (bodies that need no
+// barrier: one warp per tile).
+template <typename Body>
+__device__ __forceinline__ void warp_queue_loop(int* counter, int total, int gran, Body body)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(counter, gran);
+        t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
+        if (t0 >= total) break;
+        const int t1 = min(t0 + gran, total);
+        for (int t = t0; t < t1; t++) body(t);
+    }
+}
+
 // the frame f with base[f] <= t < base[f + 1]
 __device__ __forceinline__ int queue_frame(const uint32_t* base, int n, uint32_t t)
 {

@@ -302,6 +302,10 @@ __device__ unsigned vote_decision(const uint8_t (*s)[kHRW], int ox, int oy, int 
 
 template <int TW, int TH>
 __device__ void cc_local_core(const uint8_t* sg, int* sl, uint16_t* run, int32_t* L, int w, int h, int x0, int y0);
+template <int TW, int TH>
+__device__ void cc_sym_unions(const uint8_t* sg, int* sl);
+template <int TW, int TH>
+__device__ void cc_sym_store(const uint8_t* sg, int* sl, int32_t* L, int w, int h, int x0, int y0);
 
 // Heuristic resolution of one 64x16 tile; with L set, the tile's local
 // component labels too (union-find over the resolved bytes, still in shared
@@ -363,30 +367,43 @@ __device__ __forceinline__ void heuristics_tile(const uint8_t* snap, uint8_t* ou
         dec[by][bx] = (uint8_t)d;
     }
     __syncthreads();
+    // With L, each pixel's union-find parent starts at the leftmost pixel of
+    // its horizontal run, from one ballot of the warp that resolves the
+    // pixel's 32-pixel row segment (a warp's 32 values of k are one segment:
+    // blockDim.x is a multiple of 32 and a row is two segments); a run that
+    // comes into the second segment from the first hangs from the first
+    // segment's last pixel.
     __shared__ uint8_t res[kHTW * kHTH];
+    __shared__ int sl[kHTW * kHTH];
     for (int k = threadIdx.x; k < kHTW * kHTH; k += blockDim.x) {
         const int tx = k % kHTW, ty = k / kHTW;
         const int i = x0 + tx, j = y0 + ty;
-        if (i >= w || j >= h) {
-            res[k] = 0;
-            continue;
+        unsigned v = 0;
+        if (i < w && j < h) {
+            unsigned o = t.at(i, j);
+            // the node is the lower-right corner of block (i-1, j), the upper-right
+            // of (i-1, j-1), the upper-left of (i, j-1), the lower-left of (i, j)
+            const unsigned a = dec[ty + 1][tx], b = dec[ty][tx], c = dec[ty][tx + 1], d = dec[ty + 1][tx + 1];
+            if (a & kDecBack) o &= ~1u;
+            if (b & kDecSlash) o &= ~32u;
+            if (c & kDecBack) o &= ~128u;
+            if (d & kDecSlash) o &= ~4u;
+            out[(size_t)j * w + i] = (uint8_t)o;
+            v = o & inside_mask(i, j, w, h);
         }
-        unsigned o = t.at(i, j);
-        // the node is the lower-right corner of block (i-1, j), the upper-right
-        // of (i-1, j-1), the upper-left of (i, j-1), the lower-left of (i, j)
-        const unsigned a = dec[ty + 1][tx], b = dec[ty][tx], c = dec[ty][tx + 1], d = dec[ty + 1][tx + 1];
-        if (a & kDecBack) o &= ~1u;
-        if (b & kDecSlash) o &= ~32u;
-        if (c & kDecBack) o &= ~128u;
-        if (d & kDecSlash) o &= ~4u;
-        out[(size_t)j * w + i] = (uint8_t)o;
-        res[k] = (uint8_t)(o & inside_mask(i, j, w, h));
+        res[k] = (uint8_t)v;
+        if (L) {
+            const int lane = tx & 31;
+            const unsigned starts = __ballot_sync(0xFFFFFFFFu, tx == 0 || !bitof(v, 3));
+            const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
+            sl[k] = upto ? (k - lane) + 31 - __clz(upto) : k - lane - 1;
+        }
     }
     if (L) {
-        __shared__ int sl[kHTW * kHTH];
-        __shared__ uint16_t run[kHTW * kHTH];
         __syncthreads();
-        cc_local_core<kHTW, kHTH>(res, sl, run, L, w, h, x0, y0);
+        cc_sym_unions<kHTW, kHTH>(res, sl);
+        __syncthreads();
+        cc_sym_store<kHTW, kHTH>(res, sl, L, w, h, x0, y0);
     }
 }
 
@@ -458,8 +475,8 @@ __device__ __forceinline__ void uf_unite(int32_t* L, int a, int b)
 // are joined with one union per pair of touching runs.
 constexpr int kLT = 32;
 
-// find with path compression; parents only ever decrease, so lowering a
-// parent to the root found is safe under concurrent unions
+// find with path compression, for the passes that follow the unions (no
+// union in flight: every parent lowered is lowered to its final root)
 __device__ __forceinline__ int s_find(int* L, int x)
 {
     int r = x;
@@ -472,11 +489,23 @@ __device__ __forceinline__ int s_find(int* L, int x)
     return r;
 }
 
+// root without compression, for the unions themselves
+__device__ __forceinline__ int s_root(const int* L, int x)
+{
+    while (L[x] != x) x = L[x];
+    return x;
+}
+
+// Lock-free union, the smaller root winning. Its finds do not compress:
+// with compression interleaved with the unions of other threads, joins
+// were lost on the GPU (tile-local labels of 4096-sprite batches wrong in
+// about one tile in 10^5, one in 10^4 with volatile loads; none in 560
+// batches, 6.2 million tiles, without it).
 __device__ __forceinline__ void s_unite(int* L, int a, int b)
 {
     for (;;) {
-        a = s_find(L, a);
-        b = s_find(L, b);
+        a = s_root(L, a);
+        b = s_root(L, b);
         if (a == b) return;
         if (a > b) {
             int t = a;
@@ -486,6 +515,115 @@ __device__ __forceinline__ void s_unite(int* L, int a, int b)
         int old = atomicMin(&L[b], a);
         if (old == b) return;
         b = old;
+    }
+}
+
+// position of the set bit of rank j (from 0, counted from bit 0) of m;
+// j < popcount(m)
+__device__ __forceinline__ int nth_set_bit64(uint64_t m, int j)
+{
+    const unsigned lo = (unsigned)m;
+    const int nlo = __popc(lo);
+    return j < nlo ? (int)__fns(lo, 0, j + 1) : 32 + (int)__fns((unsigned)(m >> 32), 0, j - nlo + 1);
+}
+
+// 64-bit row mask from the ballots of a warp's two 32-pixel segments
+__device__ __forceinline__ uint64_t ballot64(bool lo, bool hi)
+{
+    return (uint64_t)__ballot_sync(0xFFFFFFFFu, lo) | (uint64_t)__ballot_sync(0xFFFFFFFFu, hi) << 32;
+}
+
+// the run start at or before position c of a line whose run starts are S
+__device__ __forceinline__ int run_start(uint64_t S, int c) { return 63 - __clzll(S & (~0ull >> (63 - c))); }
+
+// Which edges between two lines of at most 64 pixels, r and q, need a union
+// when the pixels joined along each line are already one set. Edge e at
+// position c joins r[c] and q[c + e - 1]; Sr and Sq mark where the lines'
+// runs start; q_end marks positions past the end of q (another tile, so
+// another set). An edge is skipped where another edge joins the same two
+// runs: an e = 1 edge defers to the e = 1 edge one position before it, an
+// e = 0 edge to the e = 0 or e = 1 edge one position before it, an e = 2
+// edge to the e = 2 edge one position before it or the e = 1 edge one
+// position after it, each when both runs are the same there. Every chain of
+// deferrals ends at an edge that is kept (e = 0 and e = 1 edges defer only
+// to lower positions, and an e = 2 edge to a lower position or to an e = 1
+// edge), so the kept edges join the same sets as all of them.
+__device__ __forceinline__ void join_masks(uint64_t Sr, uint64_t Sq, uint64_t E0, uint64_t E1, uint64_t E2,
+                                           uint64_t q_end, uint64_t (&need)[3])
+{
+    const uint64_t nSr = ~Sr, nSq = ~Sq;
+    need[0] = E0 & ~(nSr & (((E0 & nSq) << 1) | (E1 << 1)));
+    need[1] = E1 & ~((E1 << 1) & nSr & nSq);
+    need[2] = E2 & ~(((E2 << 1) & nSr & ~((Sq >> 1) | q_end)) | ((E1 & nSr) >> 1));
+}
+
+// fn(e, c) for every set bit c of need[e], spread over the warp's lanes
+// (one union per lane in turn)
+template <typename Fn>
+__device__ __forceinline__ void for_each_join(const uint64_t (&need)[3], Fn fn)
+{
+    const int lane = threadIdx.x & 31;
+    const int n0 = __popcll(need[0]), n01 = n0 + __popcll(need[1]), n = n01 + __popcll(need[2]);
+    for (int i = lane; i < n; i += 32) {
+        const int e = i < n0 ? 0 : i < n01 ? 1 : 2;
+        const uint64_t m = e == 0 ? need[0] : e == 1 ? need[1] : need[2];
+        fn(e, nth_set_bit64(m, i - (e == 0 ? 0 : e == 1 ? n0 : n01)));
+    }
+}
+
+// Joins of a 64-pixel-wide tile of a symmetric graph (each edge held by
+// both of its nodes, as in the resolved graph) whose parents start at the
+// run roots (a run's leftmost pixel, see heuristics_tile). A warp owns a row
+// r and joins it to row r + 1 (edges up-left, up, up-right as e = 0, 1, 2)
+// with one union per edge join_masks keeps.
+template <int TW, int TH>
+__device__ void cc_sym_unions(const uint8_t* sg, int* sl)
+{
+    static_assert(TW == 64, "two 32-pixel segments per row");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int r = warp; r < TH - 1; r += nwarp) {
+        const int p0 = r * TW + lane;
+        const unsigned a0 = sg[p0], a1 = sg[p0 + 32], b0 = sg[p0 + TW], b1 = sg[p0 + TW + 32];
+        // run starts of rows r and r + 1, edges of row r
+        const uint64_t Sr = ballot64(lane == 0 || !bitof(a0, 3), !bitof(a1, 3));
+        const uint64_t Sq = ballot64(lane == 0 || !bitof(b0, 3), !bitof(b1, 3));
+        // up-left from column 0 and up-right from column 63 leave the tile
+        uint64_t need[3];
+        join_masks(Sr, Sq, ballot64(bitof(a0, 0), bitof(a1, 0)) & ~1ull, ballot64(bitof(a0, 1), bitof(a1, 1)),
+                   ballot64(bitof(a0, 2), bitof(a1, 2)) & ~(1ull << 63), 1ull << 63, need);
+        for_each_join(need, [&](int e, int c) {
+            s_unite(sl, r * TW + run_start(Sr, c), (r + 1) * TW + run_start(Sq, c + e - 1));
+        });
+    }
+}
+
+// Labels of a tile after cc_sym_unions: one find per run (at its leftmost
+// pixel), shuffled to the run's other pixels (a run that comes into the
+// second segment takes the first segment's last label), stored as global
+// indices of the tile-local roots.
+template <int TW, int TH>
+__device__ void cc_sym_store(const uint8_t* sg, int* sl, int32_t* L, int w, int h, int x0, int y0)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int r = warp; r < TH; r += nwarp) {
+        int carry = 0;
+#pragma unroll
+        for (int sgm = 0; sgm < TW / 32; sgm++) {
+            const int c = sgm * 32 + lane, p = r * TW + c;
+            const unsigned starts = __ballot_sync(0xFFFFFFFFu, c == 0 || !bitof(sg[p], 3));
+            const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
+            const int src = upto ? 31 - __clz(upto) : 0;
+            int g = 0;
+            if (upto && src == lane) {
+                const int root = s_find(sl, p);
+                g = (y0 + root / TW) * w + (x0 + root % TW);
+            }
+            g = __shfl_sync(0xFFFFFFFFu, g, src);
+            if (!upto) g = carry;
+            carry = __shfl_sync(0xFFFFFFFFu, g, 31);
+            const int x = x0 + c, y = y0 + r;
+            if (x < w && y < h) L[(size_t)y * w + x] = g;
+        }
     }
 }
 
@@ -567,11 +705,11 @@ __global__ void __launch_bounds__(256) k_cc_local(const uint8_t* g, int32_t* L, 
 // harmless). One thread per border pixel of a tile (4 * 32 - 4 of them).
 constexpr int kLBorder = 4 * kLT - 4;
 
-// unions of border pixel q (of 2 TW + 2 (TH - 2)) of tile `tile` in a TW x TH
+// unions of border pixel q (of 4 kLT - 4) of tile `tile` in the kLT x kLT
 // tiling with neighbours in other tiles
-template <int TW, int TH, bool SYMMETRIC = false>
-__device__ __forceinline__ void cc_merge_border_t(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
+__device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
 {
+    constexpr int TW = kLT, TH = kLT;
     const int tiles_x = (w + TW - 1) / TW;
     // border position q: bottom row, top row, then left and right columns
     int lx, ly;
@@ -589,28 +727,73 @@ __device__ __forceinline__ void cc_merge_border_t(const uint8_t* g, int32_t* L, 
         int ni = i + dir_di(e), nj = j + dir_dj(e);
         if (ni < 0 || nj < 0 || ni >= w || nj >= h) continue;
         if (ni / TW == i / TW && nj / TH == j / TH) continue;
-        // a symmetric graph (the resolved graph of this pipeline) holds each
-        // pair from both ends: unite it once, from the lower index
-        if (SYMMETRIC && nj * w + ni < k) continue;
         uf_unite(L, k, nj * w + ni);
     }
 }
 
-__device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, int w, int h, int tile, int q)
+// Unions across the bottom and right borders of the 64x16 tile (tx, ty) of
+// a symmetric graph, by one warp, on the local labels. The bottom border
+// pairs row y0 + 15 with row y0 + 16 (its up-left edge from column 0 and
+// up-right edge from column 63 reach the tiles below-left and below-right);
+// the right border pairs column x0 + 63 with column x0 + 64 over the tile's
+// rows (runs along the columns: the pixels joined by the vertical edge),
+// the edges to the right, down-right (rows 0-14) and from x0 + 64 down-left
+// (rows 0-14); the two diagonals from row 15 belong to the bottom borders of
+// this tile and of the tile to the right. Every cross-tile pair is joined
+// by exactly one tile, and of the edges between the same two runs only one.
+__device__ void cc_merge_tile_warp(const uint8_t* g, int32_t* L, int w, int h, int tx, int ty)
 {
-    cc_merge_border_t<kLT, kLT>(g, L, w, h, tile, q);
+    const int lane = threadIdx.x & 31;
+    const int x0 = tx * kHTW, y0 = ty * kHTH;
+    const int yr = y0 + kHTH - 1, yq = yr + 1;
+    if (yq < h) {
+        unsigned a[2], b[2];
+#pragma unroll
+        for (int sgm = 0; sgm < 2; sgm++) {
+            const int x = x0 + 32 * sgm + lane;
+            a[sgm] = x < w ? g[(size_t)yr * w + x] & inside_mask(x, yr, w, h) : 0u;
+            b[sgm] = x < w ? g[(size_t)yq * w + x] & inside_mask(x, yq, w, h) : 0u;
+        }
+        const uint64_t Sr = ballot64(lane == 0 || !bitof(a[0], 3), !bitof(a[1], 3));
+        const uint64_t Sq = ballot64(lane == 0 || !bitof(b[0], 3), !bitof(b[1], 3));
+        uint64_t need[3];
+        join_masks(Sr, Sq, ballot64(bitof(a[0], 0), bitof(a[1], 0)), ballot64(bitof(a[0], 1), bitof(a[1], 1)),
+                   ballot64(bitof(a[0], 2), bitof(a[1], 2)), 1ull << 63, need);
+        for_each_join(need, [&](int e, int c) {
+            const int nc = c + e - 1, qc = nc < 0 || nc >= kHTW ? nc : run_start(Sq, nc);
+            uf_unite(L, yr * w + x0 + run_start(Sr, c), yq * w + x0 + qc);
+        });
+    }
+    const int xr = x0 + kHTW - 1, xq = xr + 1;
+    if (xq < w) {
+        const int y = y0 + lane;
+        unsigned a = 0, b = 0;
+        if (lane < kHTH && y < h) {
+            a = g[(size_t)y * w + xr] & inside_mask(xr, y, w, h);
+            b = g[(size_t)y * w + xq] & inside_mask(xq, y, w, h);
+        }
+        // runs along the columns: row y starts one unless row y - 1 links up
+        const uint64_t Sr = ~((uint64_t)__ballot_sync(0xFFFFFFFFu, bitof(a, 1)) << 1);
+        const uint64_t Sq = ~((uint64_t)__ballot_sync(0xFFFFFFFFu, bitof(b, 1)) << 1);
+        const uint64_t E1 = __ballot_sync(0xFFFFFFFFu, bitof(a, 4));
+        const uint64_t E2 = __ballot_sync(0xFFFFFFFFu, bitof(a, 2)) & 0x7FFFu;
+        const uint64_t E0 = (uint64_t)(__ballot_sync(0xFFFFFFFFu, bitof(b, 0)) & 0x7FFFu) << 1;
+        uint64_t need[3];
+        join_masks(Sr, Sq, E0, E1, E2, 1ull << 63, need);
+        for_each_join(need, [&](int e, int c) {
+            uf_unite(L, (y0 + run_start(Sr, c)) * w + xr, (y0 + run_start(Sq, c + e - 1)) * w + xq);
+        });
+    }
 }
 
-// border pixels of a 64x16 tile: the merge after the fused local labels
-constexpr int kHBorder = 2 * kHTW + 2 * (kHTH - 2);
-
-__global__ void k_cc_merge_h(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
+// one warp per 64x16 tile
+__global__ void __launch_bounds__(128) k_cc_merge_tiles(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
-    if (t / kHBorder >= tiles) return;
-    cc_merge_border_t<kHTW, kHTH, true>(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h,
-                                        t / kHBorder, t % kHBorder);
+    const int tiles_x = (w + kHTW - 1) / kHTW, tiles = tiles_x * ((h + kHTH - 1) / kHTH);
+    const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= tiles) return;
+    cc_merge_tile_warp(g + frame_stride * blockIdx.z, L + frame_stride * blockIdx.z, w, h, t % tiles_x,
+                       t / tiles_x);
 }
 
 __global__ void k_cc_merge(const uint8_t* g, int32_t* L, int w, int h, size_t frame_stride)
@@ -700,13 +883,12 @@ __global__ void __launch_bounds__(128) k_label_merge_queue(QueueBatch q)
     // the local labels came with the heuristics stage: its tiles, its prefix
     const QueueHeader* H = q.hdr;
     const int n = H->n;
-    queue_loop(q.counters + QC_MERGE, (int)H->total[QS_HEUR], q.gran[QS_LABEL], [&](int t) {
+    warp_queue_loop(q.counters + QC_MERGE, (int)H->total[QS_HEUR], q.gran[QS_LABEL], [&](int t) {
         const uint32_t* base = H->base + QS_HEUR * (n + 1);
         const int f = queue_frame(base, n, (uint32_t)t);
         const QueueFrame fr = H->frames[f];
-        for (int b = threadIdx.x; b < kHBorder; b += blockDim.x)
-            cc_merge_border_t<kHTW, kHTH, true>(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h,
-                                                t - (int)base[f], b);
+        const int lt = t - (int)base[f], tx = (fr.w + kHTW - 1) / kHTW;
+        cc_merge_tile_warp(q.graph_b + fr.px_off, H->labels + fr.px_off, fr.w, fr.h, lt % tx, lt / tx);
     });
 }
 
@@ -858,8 +1040,7 @@ cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, in
                                           size_t frame_stride, cudaStream_t s)
 {
     const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
-    const int borders = tiles * kHBorder;
-    k_cc_merge_h<<<dim3((borders + 127) / 128, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
+    k_cc_merge_tiles<<<dim3((tiles + 3) / 4, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
     const int n = w * h;
     k_cc_flatten<<<dim3((n + 1023) / 1024, 1, nframes), 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();

@@ -7,7 +7,9 @@ frame, through the same calls the benchmark times:
     local labels, label merge and flatten, TMA raster);
   - the full 4096-sprite uneven batch (sides ~ U[8, 64], 30 % transparent
     backgrounds), x4 with labels, through the tuned persistent tile-queue
-    path, every sprite.
+    path, every sprite;
+  - the labels of both, bit-exact in every one of repeated runs (the tile
+    unions run concurrently: a race shows in some runs only).
 Rasters bit-exact (budget: 1 LSB on 0.1 % of pixels), labels bit-exact."""
 from concurrent.futures import ThreadPoolExecutor
 
@@ -75,3 +77,65 @@ def test_4096_sprite_batch_every_sprite(cuda):
     assert len(imgs) == 4096
     rasters, labels, shape = _run_batch(cuda, imgs)
     _check_all(imgs, rasters, labels)
+
+
+def _labels_only(img):
+    h, w = img.shape[:2]
+    bgr, ws = synth.rgba_to_bgr(img)
+    return O.label_cc(O.frame(bgr, w, h, ws, 1, (48, 7, 6)).graph, w, h)
+
+
+def test_sprite_batch_labels_every_run(cuda):
+    """The component labels of the 4096-sprite batch, bit-exact in every one
+    of repeated runs at each queue granularity: the tile unions run
+    concurrently, and a union lost to a race shows up only in some runs
+    (with path compression inside the concurrent unions, about one run in
+    ten of this batch had a wrong label)."""
+    import depix
+    from test_gpu_queue import _pack
+    imgs = [np.ascontiguousarray(i) for i in synth.sprites(4096, seed=0)]
+    with ThreadPoolExecutor(max_workers=16) as ex:
+        want = np.concatenate(list(ex.map(_labels_only, imgs)))
+    buf, in_off, out_off, out_bytes = _pack(imgs, 4)
+    d_in = cuda.from_numpy(buf).cuda()
+    d_out = cuda.empty((out_bytes,), dtype=cuda.uint8, device="cuda")
+    d_lab = cuda.empty((want.size,), dtype=cuda.int32, device="cuda")
+    ws = np.array([i.shape[1] for i in imgs], np.int32)
+    hs = np.array([i.shape[0] for i in imgs], np.int32)
+    io, oo = np.array(in_off, np.uint64), np.array(out_off, np.uint64)
+    ctx = depix.Context(max(i.shape[0] * i.shape[1] for i in imgs), len(imgs))
+    try:
+        for gran in (1, 2, 4, 8):
+            ctx.set_launch_shape(gran, 32, 32)
+            for rep in range(8):
+                d_lab.fill_(-5)
+                ctx.batch(ws, hs, io, oo, d_in, depix.params(scale=4), d_out, d_lab)
+                cuda.cuda.synchronize()
+                got = d_lab.cpu().numpy()
+                assert np.array_equal(got, want), f"granularity {gran}, run {rep}: {np.count_nonzero(got != want)} labels differ"
+    finally:
+        ctx.close()
+    assert depix.take_device_faults() == 0
+
+
+def test_uniform_batch_labels_every_run(cuda):
+    """The same for the uniform 256x224 batch (grid kernels), 16 frames, 10 runs."""
+    import depix
+    W, H, N = 256, 224, 16
+    frames = [np.ascontiguousarray(synth.frame(seed)) for seed in range(N)]
+    with ThreadPoolExecutor(max_workers=16) as ex:
+        want = np.concatenate(list(ex.map(_labels_only, frames)))
+    d_in = cuda.from_numpy(np.stack(frames).reshape(-1)).cuda()
+    d_out = cuda.empty((N * W * H * 64,), dtype=cuda.uint8, device="cuda")
+    d_lab = cuda.empty((N * W * H,), dtype=cuda.int32, device="cuda")
+    ctx = depix.Context(W * H, N)
+    try:
+        for rep in range(10):
+            d_lab.fill_(-5)
+            ctx.batch(np.full(N, W, np.int32), np.full(N, H, np.int32), np.arange(N, dtype=np.uint64) * np.uint64(W * H * 4),
+                      np.arange(N, dtype=np.uint64) * np.uint64(W * H * 64), d_in, depix.params(), d_out, d_lab)
+            cuda.cuda.synchronize()
+            assert np.array_equal(d_lab.cpu().numpy(), want), f"run {rep}: labels differ"
+    finally:
+        ctx.close()
+    assert depix.take_device_faults() == 0
