@@ -90,7 +90,8 @@ def test_sprite_batch_labels_every_run(cuda):
     of repeated runs at each queue granularity: the tile unions run
     concurrently, and a union lost to a race shows up only in some runs
     (with path compression inside the concurrent unions, about one run in
-    ten of this batch had a wrong label)."""
+    ten of this batch had a wrong label). The rasters of all runs are
+    byte-identical (the raster's tile tables are built with atomics too)."""
     import depix
     from test_gpu_queue import _pack
     imgs = [np.ascontiguousarray(i) for i in synth.sprites(4096, seed=0)]
@@ -104,22 +105,30 @@ def test_sprite_batch_labels_every_run(cuda):
     hs = np.array([i.shape[0] for i in imgs], np.int32)
     io, oo = np.array(in_off, np.uint64), np.array(out_off, np.uint64)
     ctx = depix.Context(max(i.shape[0] * i.shape[1] for i in imgs), len(imgs))
+    first = None
     try:
         for gran in (1, 2, 4, 8):
             ctx.set_launch_shape(gran, 32, 32)
             for rep in range(8):
                 d_lab.fill_(-5)
+                d_out.fill_(rep)
                 ctx.batch(ws, hs, io, oo, d_in, depix.params(scale=4), d_out, d_lab)
                 cuda.cuda.synchronize()
                 got = d_lab.cpu().numpy()
                 assert np.array_equal(got, want), f"granularity {gran}, run {rep}: {np.count_nonzero(got != want)} labels differ"
+                # the rasters of every run identical too
+                if first is None:
+                    first = d_out.clone()
+                else:
+                    assert cuda.equal(d_out, first), f"granularity {gran}, run {rep}: raster differs from the first run"
     finally:
         ctx.close()
     assert depix.take_device_faults() == 0
 
 
 def test_uniform_batch_labels_every_run(cuda):
-    """The same for the uniform 256x224 batch (grid kernels), 16 frames, 10 runs."""
+    """The same for the uniform 256x224 batch (grid kernels), 16 frames, 10 runs;
+    the rasters of all runs byte-identical."""
     import depix
     W, H, N = 256, 224, 16
     frames = [np.ascontiguousarray(synth.frame(seed)) for seed in range(N)]
@@ -129,13 +138,19 @@ def test_uniform_batch_labels_every_run(cuda):
     d_out = cuda.empty((N * W * H * 64,), dtype=cuda.uint8, device="cuda")
     d_lab = cuda.empty((N * W * H,), dtype=cuda.int32, device="cuda")
     ctx = depix.Context(W * H, N)
+    first = None
     try:
         for rep in range(10):
             d_lab.fill_(-5)
+            d_out.fill_(rep)
             ctx.batch(np.full(N, W, np.int32), np.full(N, H, np.int32), np.arange(N, dtype=np.uint64) * np.uint64(W * H * 4),
                       np.arange(N, dtype=np.uint64) * np.uint64(W * H * 64), d_in, depix.params(), d_out, d_lab)
             cuda.cuda.synchronize()
             assert np.array_equal(d_lab.cpu().numpy(), want), f"run {rep}: labels differ"
+            if first is None:
+                first = d_out.clone()
+            else:
+                assert cuda.equal(d_out, first), f"run {rep}: raster differs from the first run"
     finally:
         ctx.close()
     assert depix.take_device_faults() == 0
