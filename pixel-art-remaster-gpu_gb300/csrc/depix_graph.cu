@@ -573,27 +573,54 @@ __device__ __forceinline__ void for_each_join(const uint64_t (&need)[3], Fn fn)
 
 // Joins of a 64-pixel-wide tile of a symmetric graph (each edge held by
 // both of its nodes, as in the resolved graph) whose parents start at the
-// run roots (a run's leftmost pixel, see heuristics_tile). A warp owns a row
-// r and joins it to row r + 1 (edges up-left, up, up-right as e = 0, 1, 2)
-// with one union per edge join_masks keeps.
+// run roots (a run's leftmost pixel, see heuristics_tile). Warp w owns the
+// row pairs (r, r + 1) for r = w and w + 8 (edges up-left, up, up-right as
+// e = 0, 1, 2): it parks each pair's run starts and the edges join_masks
+// keeps, then spreads the unions of both pairs over its lanes at once (one
+// round of unions for up to 32 of them, not one per pair). Blocks of 256
+// threads (8 warps).
 template <int TW, int TH>
 __device__ void cc_sym_unions(const uint8_t* sg, int* sl)
 {
-    static_assert(TW == 64, "two 32-pixel segments per row");
+    static_assert(TW == 64 && TH <= 17, "two 32-pixel segments per row, at most two row pairs per warp");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int r = warp; r < TH - 1; r += nwarp) {
+    __shared__ uint64_t pm[8][2][5]; // per warp and pair: Sr, Sq, kept edges e = 0, 1, 2
+    __shared__ int pcnt[8][7];       // per warp: prefix of the kept-edge counts
+    int npairs = 0;
+    for (int r = warp; r < TH - 1; r += nwarp, npairs++) {
         const int p0 = r * TW + lane;
         const unsigned a0 = sg[p0], a1 = sg[p0 + 32], b0 = sg[p0 + TW], b1 = sg[p0 + TW + 32];
-        // run starts of rows r and r + 1, edges of row r
         const uint64_t Sr = ballot64(lane == 0 || !bitof(a0, 3), !bitof(a1, 3));
         const uint64_t Sq = ballot64(lane == 0 || !bitof(b0, 3), !bitof(b1, 3));
-        // up-left from column 0 and up-right from column 63 leave the tile
         uint64_t need[3];
         join_masks(Sr, Sq, ballot64(bitof(a0, 0), bitof(a1, 0)) & ~1ull, ballot64(bitof(a0, 1), bitof(a1, 1)),
                    ballot64(bitof(a0, 2), bitof(a1, 2)) & ~(1ull << 63), 1ull << 63, need);
-        for_each_join(need, [&](int e, int c) {
-            s_unite(sl, r * TW + run_start(Sr, c), (r + 1) * TW + run_start(Sq, c + e - 1));
-        });
+        if (lane == 0) {
+            pm[warp][npairs][0] = Sr;
+            pm[warp][npairs][1] = Sq;
+            pm[warp][npairs][2] = need[0];
+            pm[warp][npairs][3] = need[1];
+            pm[warp][npairs][4] = need[2];
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        int t = 0;
+        for (int k = 0; k < 6; k++) {
+            pcnt[warp][k] = t;
+            t += k / 3 < npairs ? __popcll(pm[warp][k / 3][2 + k % 3]) : 0;
+        }
+        pcnt[warp][6] = t;
+    }
+    __syncwarp();
+    const int n = pcnt[warp][6];
+    for (int i = lane; i < n; i += 32) {
+        int k = 0;
+        while (k < 5 && pcnt[warp][k + 1] <= i) k++;
+        const int pr = k / 3, e = k % 3, r = warp + pr * nwarp;
+        const uint64_t* m = pm[warp][pr];
+        const int c = nth_set_bit64(m[2 + e], i - pcnt[warp][k]);
+        s_unite(sl, r * TW + run_start(m[0], c), (r + 1) * TW + run_start(m[1], c + e - 1));
     }
 }
 
