@@ -768,7 +768,9 @@ __device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, in
 // (rows 0-14); the two diagonals from row 15 belong to the bottom borders of
 // this tile and of the tile to the right. Every cross-tile pair is joined
 // by exactly one tile, and of the edges between the same two runs only one.
-__device__ void cc_merge_tile_warp(const uint8_t* g, int32_t* L, int w, int h, int tx, int ty)
+// unite(a, b) joins the sets of pixels a and b (frame indices).
+template <typename Unite>
+__device__ void merge_tile_borders(const uint8_t* g, int w, int h, int tx, int ty, Unite unite)
 {
     const int lane = threadIdx.x & 31;
     const int x0 = tx * kHTW, y0 = ty * kHTH;
@@ -788,7 +790,7 @@ __device__ void cc_merge_tile_warp(const uint8_t* g, int32_t* L, int w, int h, i
                    ballot64(bitof(a[0], 2), bitof(a[1], 2)), 1ull << 63, need);
         for_each_join(need, [&](int e, int c) {
             const int nc = c + e - 1, qc = nc < 0 || nc >= kHTW ? nc : run_start(Sq, nc);
-            uf_unite(L, yr * w + x0 + run_start(Sr, c), yq * w + x0 + qc);
+            unite(yr * w + x0 + run_start(Sr, c), yq * w + x0 + qc);
         });
     }
     const int xr = x0 + kHTW - 1, xq = xr + 1;
@@ -808,9 +810,15 @@ __device__ void cc_merge_tile_warp(const uint8_t* g, int32_t* L, int w, int h, i
         uint64_t need[3];
         join_masks(Sr, Sq, E0, E1, E2, 1ull << 63, need);
         for_each_join(need, [&](int e, int c) {
-            uf_unite(L, (y0 + run_start(Sr, c)) * w + xr, (y0 + run_start(Sq, c + e - 1)) * w + xq);
+            unite((y0 + run_start(Sr, c)) * w + xr, (y0 + run_start(Sq, c + e - 1)) * w + xq);
         });
     }
+}
+
+// the same on the global labels
+__device__ __forceinline__ void cc_merge_tile_warp(const uint8_t* g, int32_t* L, int w, int h, int tx, int ty)
+{
+    merge_tile_borders(g, w, h, tx, ty, [&](int a, int b) { uf_unite(L, a, b); });
 }
 
 // one warp per 64x16 tile
@@ -1066,9 +1074,9 @@ cudaError_t take_heuristics_fault(int* out)
 cudaError_t launch_labels_after_heuristics(const uint8_t* g, int32_t* labels, int w, int h, int nframes,
                                           size_t frame_stride, cudaStream_t s)
 {
+    const int n = w * h;
     const int tiles = ((w + kHTW - 1) / kHTW) * ((h + kHTH - 1) / kHTH);
     k_cc_merge_tiles<<<dim3((tiles + 3) / 4, 1, nframes), 128, 0, s>>>(g, labels, w, h, frame_stride);
-    const int n = w * h;
     k_cc_flatten<<<dim3((n + 1023) / 1024, 1, nframes), 256, 0, s>>>(labels, n, frame_stride);
     return cudaGetLastError();
 }

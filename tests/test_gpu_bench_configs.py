@@ -154,3 +154,33 @@ def test_uniform_batch_labels_every_run(cuda):
     finally:
         ctx.close()
     assert depix.take_device_faults() == 0
+
+
+@pytest.mark.parametrize("w,h", [(256, 224), (250, 98)])
+def test_large_uniform_batch_labels(cuda, w, h):
+    """A uniform batch of 144 frames (16 distinct, frame widths a multiple
+    of 64 and not): every frame's labels bit-exact against the oracle, the
+    same frame in every copy, over two runs."""
+    import depix
+    N, distinct = 144, 16
+    frames = [np.ascontiguousarray(synth.frame(seed, w=w, h=h)) for seed in range(distinct)]
+    with ThreadPoolExecutor(max_workers=16) as ex:
+        want = list(ex.map(_labels_only, frames))
+    batch = np.stack([frames[k % distinct] for k in range(N)])
+    d_in = cuda.from_numpy(batch.reshape(-1)).cuda()
+    d_out = cuda.empty((N * w * h * 64,), dtype=cuda.uint8, device="cuda")
+    d_lab = cuda.empty((N * w * h,), dtype=cuda.int32, device="cuda")
+    ctx = depix.Context(w * h, N)
+    try:
+        for rep in range(2):
+            d_lab.fill_(-5)
+            ctx.batch(np.full(N, w, np.int32), np.full(N, h, np.int32),
+                      np.arange(N, dtype=np.uint64) * np.uint64(w * h * 4),
+                      np.arange(N, dtype=np.uint64) * np.uint64(w * h * 64), d_in, depix.params(), d_out, d_lab)
+            cuda.cuda.synchronize()
+            got = d_lab.cpu().numpy().reshape(N, -1)
+            for k in range(N):
+                assert np.array_equal(got[k], want[k % distinct]), f"run {rep}, frame {k}: labels differ"
+    finally:
+        ctx.close()
+    assert depix.take_device_faults() == 0
