@@ -797,7 +797,8 @@ def run_stream(args, dev, stream):
     # batched + refined with warm start: a batch's eight topology setups run
     # at once (each refiner on its own stream, driven from its own host
     # thread: a setup reads its counts back), then warm start and Adam steps
-    # frame after frame (each frame starts from the previous frame's nodes)
+    # frame after frame (each frame starts from the previous frame's nodes),
+    # on a stream above the setups' in priority
     from concurrent.futures import ThreadPoolExecutor
     ctx = depix.Context(W * H, B)
     d_in = torch.empty(B * fb, dtype=torch.uint8, device=dev)
@@ -805,7 +806,16 @@ def run_stream(args, dev, stream):
     rfs = [[depix.Refiner(W * H) for _ in range(B)] for _ in range(2)]  # one set per batch parity
     cap = 4 * W * H  # nodes never exceed a few per pixel
     pos = [[torch.empty(2 * cap, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(2)]
-    side = [torch.cuda.Stream(dev) for _ in range(B)]
+    # priorities: the refinement chain first (each frame waits for the one
+    # before it), then the setups in the order the chain needs them
+    try:
+        lo, hi = torch.cuda.Stream.priority_range()
+    except Exception:
+        lo, hi = 0, 0
+    side = [torch.cuda.Stream(dev, priority=min(lo, hi + 1 + k)) for k in range(B)]
+    stream = torch.cuda.Stream(dev, priority=hi)
+    caller_stream = torch.cuda.current_stream()
+    torch.cuda.set_stream(stream)
     pool = ThreadPoolExecutor(max_workers=B)
     in_off = [k * fb for k in range(B)]
     out_off = [k * out_px * 4 for k in range(B)]
@@ -909,6 +919,8 @@ def run_stream(args, dev, stream):
     for r in rfs_flat:
         r.close()
     ctx.close()
+    torch.cuda.synchronize()
+    torch.cuda.set_stream(caller_stream)
     pct = lambda v, q: round(v[min(len(v) - 1, int(q * len(v)))], 4)
     return {"workload": f"{n} frames 256x224 (background + 24 sprites at 0-3 px/frame, wrap-around), x4; "
                         f"refinement: 20 Adam steps per frame, warm start by 16x16 tile signature",
