@@ -796,7 +796,7 @@ def run_stream(args, dev, stream):
 
     # batched + refined with warm start: a batch's eight topology setups run
     # at once (each refiner on its own stream, driven from its own host
-    # thread: a setup reads its counts back), then warm start and Adam steps
+    # thread: a setup reads two counts back), then warm start and Adam steps
     # frame after frame (each frame starts from the previous frame's nodes),
     # on a stream above the setups' in priority
     from concurrent.futures import ThreadPoolExecutor
@@ -804,7 +804,7 @@ def run_stream(args, dev, stream):
     d_in = torch.empty(B * fb, dtype=torch.uint8, device=dev)
     d_out = torch.empty(B * out_px * 4, dtype=torch.uint8, device=dev)
     rfs = [[depix.Refiner(W * H) for _ in range(B)] for _ in range(2)]  # one set per batch parity
-    cap = 4 * W * H  # nodes never exceed a few per pixel
+    cap = (4 * W + 3) * (4 * H + 3)  # nodes are vertices of the quarter-unit grid
     pos = [[torch.empty(2 * cap, dtype=torch.float32, device=dev) for _ in range(B)] for _ in range(2)]
     # priorities: the refinement chain first (each frame waits for the one
     # before it), then the setups in the order the chain needs them
@@ -823,7 +823,6 @@ def run_stream(args, dev, stream):
     def setup(rf, k, uploaded):
         side[k].wait_event(uploaded)
         rf.setup(d_in[k * fb:], W, H, 4 * W, depix.LAYOUT_RGBA, None, p, rp, stream=side[k])
-        assert rf.counts()["nodes"] <= cap
         done = torch.cuda.Event(enable_timing=True)
         done.record(side[k])
         return done

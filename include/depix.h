@@ -333,11 +333,18 @@ depix_status depix_refiner_destroy(depix_refiner* r);
  * the refiner resolves the graph itself): nodes, curve edges, Chaikin
  * segments, the output samples near each segment and their targets, and a
  * signature per 16x16-pixel tile (graph bytes and colours of the tile and its
- * one-pixel ring). Synchronises the stream (reads counts back). */
+ * one-pixel ring). Reads two counts back once (edges and nodes, which size
+ * the node and segment arrays), so the call waits for the stream's work up
+ * to that point; the rest of the setup is queued on s without waiting (later
+ * calls on s see the frame; work on another stream waits for an event
+ * recorded on s). Nodes are vertices of the (4w+3) x (4h+3) quarter-pixel
+ * grid, so position buffers of that many float2 always hold a frame. */
 depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, int h, int widthstep,
                                 depix_layout layout, const uint8_t* d_graph, const depix_params* p,
                                 const depix_refine_params* rp, depix_stream s);
-/* nodes, free nodes, curve edges, segment slots, assigned samples */
+/* nodes, free nodes, curve edges, segment slots, assigned samples (the
+ * first call after a setup synchronises the device to read the counts the
+ * setup left on it) */
 depix_status depix_refine_counts(depix_refiner* r, long long counts[5]);
 /* The frozen topology to host arrays (any may be NULL): node quarter-pixel
  * coordinates (2 per node), flags (bit 0 pinned, 1 frame, 2 corner, degree

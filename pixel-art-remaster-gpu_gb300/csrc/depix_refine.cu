@@ -466,10 +466,10 @@ __global__ void k_rf_sort_samples(const int* seg_off, int S, int* samp)
 
 // the nearest-neighbour target under the coverage Gaussian, per sample
 // (separable: three column and three row weights)
-__global__ void k_rf_targets(Geo G, int scale, float sig, const int* samp, int M, float4* tgt)
+__global__ void k_rf_targets(Geo G, int scale, float sig, const int* samp, const int* pM, float4* tgt)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
+    if (m >= *pM) return;
     const int ow = G.w * scale;
     const int yo = samp[m] / ow, xo = samp[m] - yo * ow;
     const float x = ((float)xo + 0.5f) / (float)scale, y = ((float)yo + 0.5f) / (float)scale;
@@ -864,12 +864,19 @@ __global__ void k_rf_live_scatter(const int* flag, const int* pos, int S, const 
         live[pos[s]] = LiveSeg{seg[s], make_int4(seg_off[s], seg_off[s + 1], (int)col[s].x, (int)col[s].y)};
 }
 
-__global__ void k_rf_sample_xy(const int* samp, int M, int ow, int scale, float2* sxy)
+__global__ void k_rf_sample_xy(const int* samp, const int* pM, int ow, int scale, float2* sxy)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
+    if (m >= *pM) return;
     const int yo = samp[m] / ow, xo = samp[m] - yo * ow;
     sxy[m] = make_float2(((float)xo + 0.5f) / (float)scale, ((float)yo + 0.5f) / (float)scale);
+}
+
+// the step kernels' frame record, from the scan totals on the device (F in
+// slot 3, L in slot 4)
+__global__ void k_rf_frame(const int* totals, int N, int ow, int oh, int scale, float inv_samples3, RefineFrame* fr)
+{
+    *fr = RefineFrame{N, totals[4], ow, oh, scale, totals[3], inv_samples3};
 }
 
 __global__ void k_rf_free_flags(const int* flags, int N, int* is_free)
@@ -893,14 +900,17 @@ template <typename T>
 struct DevBuf {
     T* p = nullptr;
     size_t cap = 0;
+    // grows with a quarter of headroom, so that frames of about the same
+    // size reuse the buffer (a free in between would synchronize the device)
     cudaError_t reserve(size_t n)
     {
         if (n <= cap && p) return cudaSuccess;
         dev_free(p);
         p = nullptr;
         cap = 0;
-        cudaError_t e = dev_alloc(&p, std::max<size_t>(n, 1) * sizeof(T));
-        if (e == cudaSuccess) cap = n;
+        const size_t want = std::max<size_t>(n + n / 4, 1);
+        cudaError_t e = dev_alloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
         return e;
     }
     void release()
@@ -924,7 +934,8 @@ struct depix_refiner {
     const uint64_t* lut = nullptr;
     // frame
     int w = 0, h = 0, scale = 0, ow = 0, oh = 0;
-    int E = 0, N = 0, F = 0, S = 0, M = 0;
+    int E = 0, N = 0, F = 0, S = 0, M = 0; // F, M and L: -1 until read back (fetch_counts)
+    int max_split = 0; // split curve edges a cell can own at most (its hull box's lattice steps)
     float sigma = 0.5f; // coverage sigma of the targets (output pixels)
     DevBuf<uint32_t> vgrid;
     DevBuf<uint32_t> box;
@@ -953,7 +964,6 @@ struct depix_refiner {
     int L = 0;
     int* h_scalars = nullptr; // pinned
     double* h_energy = nullptr;
-    RefineFrame* h_frame = nullptr;
     bool ready = false;
     // the Adam loop as a graph, replayed while its parameters and buffers stay
     cudaStream_t capture_stream = nullptr;
@@ -985,12 +995,25 @@ depix_status rf_fail(cudaError_t e, const char* where)
 
 int blocks_for(long long n, int t = 256) { return (int)std::max<long long>(1, (n + t - 1) / t); }
 
-// total of the last exclusive scan, read back to the host (synchronous)
-depix_status read_total(depix_refiner* r, int slot, int* out, cudaStream_t s)
+// scan totals in slots [slot, slot + n), read back to the host (synchronous)
+depix_status read_totals(depix_refiner* r, int slot, int n, int* out, cudaStream_t s)
 {
-    RF_CK(cudaMemcpyAsync(r->h_scalars + slot, r->scalars.p + slot, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RF_CK(cudaMemcpyAsync(r->h_scalars + slot, r->scalars.p + slot, n * sizeof(int), cudaMemcpyDeviceToHost, s));
     RF_CK(cudaStreamSynchronize(s));
-    *out = r->h_scalars[slot];
+    for (int k = 0; k < n; k++) out[k] = r->h_scalars[slot + k];
+    return DEPIX_OK;
+}
+
+// M, F and L of the set-up frame (scan totals left on the device by the
+// setup), read back when a caller asks for them
+depix_status fetch_counts(depix_refiner* r)
+{
+    if (r->M >= 0) return DEPIX_OK;
+    RF_CK(cudaDeviceSynchronize());
+    RF_CK(cudaMemcpy(r->h_scalars + 2, r->scalars.p + 2, 3 * sizeof(int), cudaMemcpyDeviceToHost));
+    r->M = r->h_scalars[2];
+    r->F = r->h_scalars[3];
+    r->L = r->h_scalars[4];
     return DEPIX_OK;
 }
 
@@ -1063,9 +1086,9 @@ int pow2_at_least(long long n)
 }
 int cov_blocks(const depix_refiner* r)
 {
-    return std::min(r->sms * 8, pow2_at_least(((long long)r->L * kSegLanes + 255) / 256));
+    return std::min(r->sms * 8, pow2_at_least(((long long)r->S * kSegLanes + 255) / 256)); // L <= S
 }
-int node_blocks(const depix_refiner* r) { return std::min(r->sms * 8, pow2_at_least(((long long)r->F + 255) / 256)); }
+int node_blocks(const depix_refiner* r) { return std::min(r->sms * 8, pow2_at_least(((long long)r->N + 255) / 256)); } // F <= N
 
 bool same_loop(const StepArgs& a, const StepArgs& b)
 {
@@ -1161,11 +1184,23 @@ depix_status depix_refiner_create(depix_refiner** out, size_t max_pixels)
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
+    if (e == cudaSuccess) {
+        // A cell's split curve edges lie on its convex hull, at most one per
+        // quarter-unit lattice step: at most 2 (width + height) of the hull's
+        // box, over all patterns.
+        std::vector<uint32_t> box(4096);
+        e = cudaMemcpy(box.data(), r->box.p, 4096 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        for (uint32_t b : box) {
+            if (b == 0xFFu) continue;
+            const int x0 = (int)(b & 0xFF), x1 = (int)((b >> 8) & 0xFF), y0 = (int)((b >> 16) & 0xFF), y1 = (int)(b >> 24);
+            r->max_split = std::max(r->max_split, 2 * ((x1 - x0) + (y1 - y0)));
+        }
+        r->max_split = std::max(r->max_split, 1);
+    }
     if (e == cudaSuccess) e = r->scalars.reserve(8);
     if (e == cudaSuccess) e = r->energy.reserve(3);
     if (e == cudaSuccess) e = cudaHostAlloc(&r->h_scalars, 8 * sizeof(int), cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaHostAlloc(&r->h_energy, 4 * sizeof(double), cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaHostAlloc(&r->h_frame, sizeof(RefineFrame), cudaHostAllocDefault);
     if (e == cudaSuccess) e = r->frame.reserve(1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1198,7 +1233,6 @@ depix_status depix_refiner_destroy(depix_refiner* r)
     r->free_flag.release(); r->free_pos.release(); r->fnodes.release(); r->sxy.release();
     if (r->loop) cudaGraphExecDestroy(r->loop);
     if (r->capture_stream) cudaStreamDestroy(r->capture_stream);
-    cudaFreeHost(r->h_frame);
     cudaFreeHost(r->h_scalars);
     cudaFreeHost(r->h_energy);
     delete r;
@@ -1257,15 +1291,17 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     k_rf_count_edges<<<blocks_for(n, 128), 128, 0, s>>>(G, r->vgrid.p, r->cell_count.p);
     RF_CK(cudaGetLastError());
     RF_CK(exclusive_scan(r->cell_count.p, r->cell_off.p, n, r->tile_sums.p, r->scalars.p + 0, s));
-    int E = 0;
-    DEPIX_TRY_RF(read_total(r, 0, &E, s));
-    RF_CK(r->edges.reserve(E));
+    // edges reserved for the most a frame can have, so that E and N come
+    // back together: the one read back of the setup (they size the node and
+    // segment arrays; the later counts stay on the device)
+    RF_CK(r->edges.reserve((size_t)n * r->max_split));
     k_rf_emit_edges<<<blocks_for(n, 128), 128, 0, s>>>(G, r->vgrid.p, r->cell_off.p, r->edges.p, r->nb_v.p, r->nb_e.p);
     k_rf_node_flags<<<blocks_for(nv), 256, 0, s>>>(r->vgrid.p, nv, r->is_node.p);
     RF_CK(cudaGetLastError());
     RF_CK(exclusive_scan(r->is_node.p, r->nid.p, nv, r->tile_sums.p, r->scalars.p + 1, s));
-    int N = 0;
-    DEPIX_TRY_RF(read_total(r, 1, &N, s));
+    int EN[2];
+    DEPIX_TRY_RF(read_totals(r, 0, 2, EN, s));
+    const int E = EN[0], N = EN[1];
     RF_CK(r->node_q.reserve(N));
     RF_CK(r->node_flags.reserve(N));
     RF_CK(r->node_nbr.reserve(N));
@@ -1302,17 +1338,17 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     k_rf_count_samples<<<blocks_for(no_px), 256, 0, s>>>(r->bseg.p, no_px, r->seg_count.p);
     RF_CK(cudaGetLastError());
     RF_CK(exclusive_scan(r->seg_count.p, r->seg_off.p, S + 1, r->tile_sums.p, r->scalars.p + 2, s));
-    int M = 0;
-    DEPIX_TRY_RF(read_total(r, 2, &M, s));
-    RF_CK(r->samp.reserve(M));
-    RF_CK(r->tgt.reserve(M));
+    // samples (M on the device): at most one per output pixel
+    RF_CK(r->samp.reserve(no_px));
+    RF_CK(r->tgt.reserve(no_px));
     RF_CK(cudaMemsetAsync(r->cursor.p, 0, ((size_t)S + 1) * sizeof(int), s));
     k_rf_scatter_samples<<<blocks_for(no_px), 256, 0, s>>>(r->bseg.p, no_px, r->seg_off.p, r->cursor.p, r->samp.p);
     k_rf_sort_samples<<<blocks_for(S), 256, 0, s>>>(r->seg_off.p, S, r->samp.p);
-    k_rf_targets<<<blocks_for(M), 256, 0, s>>>(G, p->scale, rp->sigma / (float)p->scale, r->samp.p, M, r->tgt.p);
+    k_rf_targets<<<blocks_for(no_px), 256, 0, s>>>(G, p->scale, rp->sigma / (float)p->scale, r->samp.p,
+                                                   r->scalars.p + 2, r->tgt.p);
     RF_CK(cudaGetLastError());
-    RF_CK(r->sxy.reserve(M));
-    k_rf_sample_xy<<<blocks_for(M), 256, 0, s>>>(r->samp.p, M, ow, p->scale, r->sxy.p);
+    RF_CK(r->sxy.reserve(no_px));
+    k_rf_sample_xy<<<blocks_for(no_px), 256, 0, s>>>(r->samp.p, r->scalars.p + 2, ow, p->scale, r->sxy.p);
     // free nodes and their curvature stencils
     RF_CK(r->free_flag.reserve(N));
     RF_CK(r->free_pos.reserve(N));
@@ -1324,8 +1360,6 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
                                                   r->fnodes.p);
     RF_CK(cudaGetLastError());
     RF_CK(cudaMemsetAsync(r->gcov.p, 0, (size_t)std::max(N, 1) * sizeof(float2), s));
-    int F = 0;
-    DEPIX_TRY_RF(read_total(r, 3, &F, s));
     r->w = w;
     r->h = h;
     r->scale = p->scale;
@@ -1333,9 +1367,8 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     r->oh = oh;
     r->E = E;
     r->N = N;
-    r->F = F;
     r->S = S;
-    r->M = M;
+    r->F = r->M = r->L = -1; // on the device until fetch_counts
     r->sigma = rp->sigma;
     // live segments
     RF_CK(r->live_flag.reserve(S));
@@ -1352,13 +1385,10 @@ depix_status depix_refine_setup(depix_refiner* r, const uint8_t* d_img, int w, i
     RF_CK(r->tile_hash.reserve(r->tiles));
     k_rf_tile_hash<<<blocks_for(r->tiles, 64), 64, 0, s>>>(G, r->tiles_x, r->tiles, r->tile_hash.p);
     RF_CK(cudaGetLastError());
-    int L = 0;
-    DEPIX_TRY_RF(read_total(r, 4, &L, s));
-    r->L = L;
-    *r->h_frame = RefineFrame{N, L, ow, oh, p->scale, F, (float)(1.0 / (3.0 * (double)ow * (double)oh))};
-    RF_CK(cudaMemcpyAsync(r->frame.p, r->h_frame, sizeof(RefineFrame), cudaMemcpyHostToDevice, s));
-    RF_CK(cudaStreamSynchronize(s));
-    r->ready = true;
+    k_rf_frame<<<1, 1, 0, s>>>(r->scalars.p, N, ow, oh, p->scale, (float)(1.0 / (3.0 * (double)ow * (double)oh)),
+                               r->frame.p);
+    RF_CK(cudaGetLastError());
+    r->ready = true; // the rest is ordered on s: later calls on s see the frame, others wait on an event of s
     return DEPIX_OK;
 }
 
@@ -1369,6 +1399,7 @@ depix_status depix_refine_counts(depix_refiner* r, long long counts[5])
         set_last_error("NULL counts");
         return DEPIX_ERR_INVALID_ARG;
     }
+    DEPIX_TRY_RF(fetch_counts(r));
     counts[0] = r->N;
     counts[1] = r->F;
     counts[2] = r->E;
@@ -1381,7 +1412,7 @@ depix_status depix_refine_export(depix_refiner* r, int32_t* node_q, int32_t* nod
                                  int32_t* edges, int32_t* segs, uint32_t* seg_colors, int32_t* samples)
 {
     DEPIX_TRY_RF(check_refiner(r));
-    RF_CK(cudaDeviceSynchronize());
+    DEPIX_TRY_RF(fetch_counts(r));
     if (node_q) RF_CK(cudaMemcpy(node_q, r->node_q.p, (size_t)r->N * sizeof(int2), cudaMemcpyDeviceToHost));
     if (node_flags) RF_CK(cudaMemcpy(node_flags, r->node_flags.p, (size_t)r->N * sizeof(int), cudaMemcpyDeviceToHost));
     if (node_nbr) RF_CK(cudaMemcpy(node_nbr, r->node_nbr.p, (size_t)r->N * sizeof(int2), cudaMemcpyDeviceToHost));
@@ -1457,7 +1488,7 @@ depix_status depix_refine_warm_start(depix_refiner* r, const depix_refiner* prev
         k_rf_same_tiles<<<blocks_for(r->tiles), 256, 0, s>>>(r->tile_hash.p, prev->tile_hash.p, r->tiles,
                                                              r->scalars.p + 5);
         RF_CK(cudaGetLastError());
-        DEPIX_TRY_RF(read_total(r, 5, reused_tiles, s));
+        DEPIX_TRY_RF(read_totals(r, 5, 1, reused_tiles, s));
     }
     return DEPIX_OK;
 }
