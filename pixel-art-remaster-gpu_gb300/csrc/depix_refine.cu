@@ -872,6 +872,18 @@ __global__ void k_rf_sample_xy(const int* samp, const int* pM, int ow, int scale
     sxy[m] = make_float2(((float)xo + 0.5f) / (float)scale, ((float)yo + 0.5f) / (float)scale);
 }
 
+// start of an Adam run: both position buffers from src, moments zeroed
+__global__ void k_rf_begin(const float2* src, float2* x, float2* y, float2* m, float2* v, int N)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const float2 q = src[i];
+        x[i] = q;
+        y[i] = q; // pinned nodes never move: both buffers start equal
+        m[i] = make_float2(0.f, 0.f);
+        v[i] = make_float2(0.f, 0.f);
+    }
+}
+
 // the step kernels' frame record, from the scan totals on the device (F in
 // slot 3, L in slot 4)
 __global__ void k_rf_frame(const int* totals, int N, int ow, int oh, int scale, float inv_samples3, RefineFrame* fr)
@@ -1517,12 +1529,9 @@ depix_status depix_refine_run(depix_refiner* r, const depix_refine_params* p, fl
     const size_t bytes = (size_t)r->N * sizeof(float2);
     float2* x = r->pos_a.p;
     float2* y = r->pos_b.p;
-    RF_CK(cudaMemcpyAsync(x, d_pos ? reinterpret_cast<const float2*>(d_pos) : r->pos0.p, bytes,
-                          cudaMemcpyDeviceToDevice, s));
-    // pinned nodes never move: both buffers start equal
-    RF_CK(cudaMemcpyAsync(y, x, bytes, cudaMemcpyDeviceToDevice, s));
-    RF_CK(cudaMemsetAsync(r->adam_m.p, 0, bytes, s));
-    RF_CK(cudaMemsetAsync(r->adam_v.p, 0, bytes, s));
+    k_rf_begin<<<std::min(blocks_for(r->N), r->sms * 4), 256, 0, s>>>(
+        d_pos ? reinterpret_cast<const float2*>(d_pos) : r->pos0.p, x, y, r->adam_m.p, r->adam_v.p, r->N);
+    RF_CK(cudaGetLastError());
     if (before) DEPIX_TRY_RF(eval(r, p, x, nullptr, before, s));
     const StepArgs a = step_args(r, p);
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
