@@ -286,14 +286,23 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(2):
         ctx.batch_host(ws, hs, in_off, out_off, h_in, h_in.numel(), p, h_out, h_out.numel(), h_lab, stream=stream)
     barrier()
+    step_ms = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
+        # returns when the step's last copy to host memory is done
         ctx.batch_host(ws, hs, in_off, out_off, h_in, h_in.numel(), p, h_out, h_out.numel(), h_lab, stream=stream)
+        step_ms.append((time.perf_counter() - ts) * 1e3)
     e2e_s = time.perf_counter() - t0
     e2e_v = replicas.job_throughput(B * e2e_steps, e2e_s, dev)
+    step_ms.sort()
+    # value: all timed steps; the per-step spread shows when the shared host
+    # link was busy with other traffic during some steps
     e2e = {"value": round(e2e_v, 1), "unit": UNIT, "h2d_bytes_per_step": B * in_bytes,
            "d2h_bytes_per_step": B * (out_px * 4 + W * H * 4), "steps": e2e_steps,
-           "timed_s": round(e2e_s, 3)}
+           "timed_s": round(e2e_s, 3), "step_ms": {"min": round(step_ms[0], 2),
+                                                  "median": round(step_ms[len(step_ms) // 2], 2),
+                                                  "max": round(step_ms[-1], 2)}}
 
     # frames of both paths against the CPU oracle (a C restatement of the
     # reference's stage bodies): rasters and labels of a few frames of the
