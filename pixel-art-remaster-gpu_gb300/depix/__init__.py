@@ -377,7 +377,8 @@ class Refiner:
                                         ctypes.byref(rp), stream_ptr(stream)), "depix_refine_setup")
 
     def counts(self):
-        """dict of nodes, free, edges, segments (slots), samples."""
+        """dict of nodes, free, edges, segments (slots), samples (the first
+        call after a setup synchronises the device)."""
         c = (ctypes.c_longlong * 5)()
         _check(lib().depix_refine_counts(self.handle, c), "depix_refine_counts")
         return dict(zip(("nodes", "free", "edges", "segments", "samples"), list(c)))
