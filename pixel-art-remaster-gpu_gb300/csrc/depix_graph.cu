@@ -467,12 +467,15 @@ __device__ __forceinline__ void uf_unite(int32_t* L, int a, int b)
     }
 }
 
-// Component labels in three passes: union-find inside 32x32 tiles in shared
-// memory (local roots are the tile-local minima, which are also the minima in
-// global index order), then unions across tile borders on the global label
-// array, then one flattening pass. Inside a tile a warp owns a row: horizontal
-// runs come from one ballot (a run's root is its leftmost pixel), and rows
-// are joined with one union per pair of touching runs.
+// Component labels in three passes: union-find inside tiles in shared memory
+// (local roots are the tile-local minima, which are also the minima in global
+// index order), then unions across tile borders on the global label array,
+// then one flattening pass. The frame and batch paths make the tile-local
+// labels inside the 64x16 heuristics tiles (cc_sym_unions, cc_sym_store) and
+// merge with merge_tile_borders; the stage API (depix_label_components) runs
+// its own 32x32 tiles over a graph in global memory (cc_local_core: a warp
+// owns a row, horizontal runs from one ballot, one union per pair of touching
+// runs).
 constexpr int kLT = 32;
 
 // find with path compression, for the passes that follow the unions (no
@@ -758,16 +761,17 @@ __device__ __forceinline__ void cc_merge_border(const uint8_t* g, int32_t* L, in
     }
 }
 
-// Unions across the bottom and right borders of the 64x16 tile (tx, ty) of
-// a symmetric graph, by one warp, on the local labels. The bottom border
-// pairs row y0 + 15 with row y0 + 16 (its up-left edge from column 0 and
-// up-right edge from column 63 reach the tiles below-left and below-right);
-// the right border pairs column x0 + 63 with column x0 + 64 over the tile's
-// rows (runs along the columns: the pixels joined by the vertical edge),
-// the edges to the right, down-right (rows 0-14) and from x0 + 64 down-left
-// (rows 0-14); the two diagonals from row 15 belong to the bottom borders of
-// this tile and of the tile to the right. Every cross-tile pair is joined
-// by exactly one tile, and of the edges between the same two runs only one.
+// Unions across two borders of the 64x16 tile (tx, ty) of a symmetric
+// graph, by one warp. Rows y0 + 15 and y0 + 16: the edges from row y0 + 15
+// to (x - 1, y + 1), (x, y + 1), (x + 1, y + 1), the first reaching from
+// column x0 into the tile at (tx - 1, ty + 1) and the last from column
+// x0 + 63 into (tx + 1, ty + 1). Columns x0 + 63 and x0 + 64 over rows
+// y0 .. y0 + 15 (runs along the columns: the pixels joined by their (x, y + 1)
+// edge): the edges (x + 1, y) of every row, (x + 1, y + 1) of rows y0 ..
+// y0 + 14 and, from column x0 + 64, (x - 1, y + 1) of those rows; the two
+// diagonals from row y0 + 15 belong to the row pairs of this tile and of
+// tile (tx + 1, ty). Every cross-tile pair is joined by exactly one tile, and
+// of the edges between the same two runs only one (join_masks).
 // unite(a, b) joins the sets of pixels a and b (frame indices).
 template <typename Unite>
 __device__ void merge_tile_borders(const uint8_t* g, int w, int h, int tx, int ty, Unite unite)
