@@ -301,3 +301,69 @@ def test_setup_resolves_the_graph_itself(cuda):
         assert np.array_equal(g1[k], g2[k]), k
     rf.close()
     rf2.close()
+
+
+def test_setups_on_side_streams_then_a_warm_started_chain(cuda):
+    """Setups that return before their work is done: four frames of a stream
+    set up at once, each on its own stream (the graph resolved by the
+    refiner), then initial / warm start and 20 steps frame after frame on a
+    third stream that waits on each setup's event. Topologies bit-exact
+    against the specification; every frame's energy lowered by its steps and
+    within 1 % of the same calls made one after another on one stream (the
+    coverage gradient is summed with float atomics, whose order, and through
+    Adam's normalised step the positions, depend on what else runs);
+    positions finite and within Adam's reach of their start."""
+    import depix
+    torch = cuda
+    w, h = 128, 96
+    frames = synth.stream(4, seed=1, n_sprites=2, w=w, h=h)
+    d_imgs = [torch.from_numpy(np.ascontiguousarray(f).reshape(-1).copy()).cuda() for f in frames]
+    rp = depix.refine_params(steps=20)
+    p = depix.params()
+    cap = 2 * (4 * w + 3) * (4 * h + 3)
+
+    def chain(rfs, setup_streams, main):
+        done = []
+        for k, rf in enumerate(rfs):
+            rf.setup(d_imgs[k], w, h, 4 * w, depix.LAYOUT_RGBA, None, p, rp, stream=setup_streams[k])
+            ev = torch.cuda.Event()
+            ev.record(setup_streams[k])
+            done.append(ev)
+        pos = [torch.zeros(cap, dtype=torch.float32, device="cuda") for _ in rfs]
+        start = [torch.zeros(cap, dtype=torch.float32, device="cuda") for _ in rfs]
+        for k, rf in enumerate(rfs):
+            main.wait_event(done[k])
+            if k == 0:
+                rf.initial(pos[k], stream=main)
+            else:
+                rf.warm_start(rfs[k - 1], pos[k - 1], pos[k], stream=main, count=False)
+            with torch.cuda.stream(main):
+                start[k].copy_(pos[k])
+            rf.run(rp, pos[k], stream=main, energies=False)
+        torch.cuda.synchronize()
+        return pos, start
+
+    side = [torch.cuda.Stream() for _ in frames]
+    main = torch.cuda.Stream()
+    rfs = [depix.Refiner(w * h) for _ in frames]
+    got, got_start = chain(rfs, side, main)
+    one = torch.cuda.current_stream()
+    rfs_seq = [depix.Refiner(w * h) for _ in frames]
+    want, _ = chain(rfs_seq, [one] * len(frames), one)
+    for k, f in enumerate(frames):
+        bgr, ws = synth.rgba_to_bgr(f)
+        raw, _, res = O.graph(bgr, w, h, ws, (48, 7, 6))
+        top = R.topology(f, res, raw, 4)
+        _compare_topology(rfs[k].export(), top)
+        n = 2 * len(top.qx)
+        assert bool(torch.isfinite(got[k][:n]).all()), f"frame {k}"
+        # an Adam step moves a coordinate by at most lr (1 - beta1) / sqrt(1 - beta2) = 3.16 lr
+        assert float((got[k][:n] - got_start[k][:n]).abs().max()) <= 20 * rp.lr * 3.2, f"frame {k}"
+        assert bool(torch.all(got[k][n:] == 0)), f"frame {k}: written past its nodes"
+        e_start = rfs[k].energy_grad(rp, got_start[k])[3]
+        e_got = rfs[k].energy_grad(rp, got[k])[3]
+        e_want = rfs_seq[k].energy_grad(rp, want[k])[3]
+        assert e_got < e_start, f"frame {k}"
+        assert abs(e_got - e_want) <= 1e-2 * e_want, f"frame {k}: {e_got} against {e_want}"
+    for rf in rfs + rfs_seq:
+        rf.close()
